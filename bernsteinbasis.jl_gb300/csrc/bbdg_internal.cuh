@@ -1,0 +1,245 @@
+// Internal declarations shared by the bbdg CUDA translation units (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/bbdg.h"
+
+// ------------------------------------------------------------------------------------
+// Degree bookkeeping. Multi-indices follow src/ordering.jl: 3D coefficients are ordered
+// k (outer), j, i (inner); 2D coefficients j (outer), i (inner).
+// ------------------------------------------------------------------------------------
+__host__ __device__ __forceinline__ int64_t min64(int64_t a, int64_t b) { return a < b ? a : b; }
+__host__ __device__ __forceinline__ int np2(int n) { return n < 0 ? 0 : (n + 1) * (n + 2) / 2; }
+__host__ __device__ __forceinline__ int np3(int n) {
+  return n < 0 ? 0 : (n + 1) * (n + 2) * (n + 3) / 6;
+}
+// Row offset of row j in the degree-n triangle (ordering.jl:8-16, 0-based).
+__host__ __device__ __forceinline__ int tri_off(int n, int j) { return j * (2 * n + 3 - j) / 2; }
+// Layer offset of layer k in the degree-n tetrahedron (ordering.jl:18-26):
+// sum_{m=1..k} T(n+2-m) = tet(n+1) - tet(n+1-k), T/tet the triangular/tetrahedral numbers.
+__host__ __device__ __forceinline__ int tet_off(int n, int k) {
+  const int a = n + 1, b = n + 1 - k;
+  return (a * (a + 1) * (a + 2) - b * (b + 1) * (b + 2)) / 6;
+}
+__host__ __device__ __forceinline__ int ij2(int n, int i, int j) { return i + tri_off(n, j); }
+// ordering.jl:32-35, 0-based.
+__host__ __device__ __forceinline__ int ijk3(int n, int i, int j, int k) {
+  return i + tri_off(n, j) + tet_off(n, k) - j * k;
+}
+
+// Face f's node (a, b) at distance d from the face (layer d), as a 3D index of degree N.
+// f0: j=0 face (i,k,j) -> (a,d,b); f1: l=0 face (j,k,l); f2: i=0 face (j,k,i);
+// f3: k=0 face (i,j,k). These are the permutations of src/BernsteinLift.jl:207-218.
+__host__ __device__ __forceinline__ int face_vol(int N, int f, int a, int b, int d) {
+  switch (f) {
+    case 0: return ijk3(N, a, d, b);
+    case 1: return ijk3(N, N - a - b - d, a, b);
+    case 2: return ijk3(N, d, a, b);
+    default: return ijk3(N, a, b, d);
+  }
+}
+
+// Device-resident lookup tables of one degree, built once per context.
+struct DegTables {
+  int N = 0, Np = 0, NpM1 = 0, Nfp = 0;
+  // word offsets inside `words` (uint32 units)
+  int o_node3 = 0;   // Np   packed (i | j<<8 | k<<16), degree N
+  int o_node3m1 = 0; // NpM1 packed, degree N-1
+  int o_node2 = 0;   // np3(N+1) uint16 (a | b<<8), 2D decode of degrees 0..N+1; degree n
+                     // starts at np3(n-1)
+  int o_fvol = 0;    // 4*Nfp uint16: face node -> volume index
+  int o_fperm = 0;   // 6*Nfp uint16: face node -> neighbour face node, per orientation
+  int nwords = 0;
+  uint32_t* d_words = nullptr;
+  double* d_lj = nullptr;  // N+1 entries, d_lj[j] = l_j(N) (constants.jl:10-12), [0] = 0
+  float* d_ljf = nullptr;
+};
+
+// Orientation codes: face vertex m of this side is face vertex PERMS[o][m] of the partner,
+// PERMS = (0,1,2),(0,2,1),(1,0,2),(1,2,0),(2,0,1),(2,1,0), packed 2 bits per entry.
+__host__ __device__ __forceinline__ int perm_of(int o, int m) {
+  constexpr uint64_t kPack = (0ull << 0) | (1ull << 2) | (2ull << 4) |     // (0,1,2)
+                             (0ull << 6) | (2ull << 8) | (1ull << 10) |    // (0,2,1)
+                             (1ull << 12) | (0ull << 14) | (2ull << 16) |  // (1,0,2)
+                             (1ull << 18) | (2ull << 20) | (0ull << 22) |  // (1,2,0)
+                             (2ull << 24) | (0ull << 26) | (1ull << 28) |  // (2,0,1)
+                             (2ull << 30) | (1ull << 32) | (0ull << 34);   // (2,1,0)
+  return int((kPack >> (2 * (3 * o + m))) & 3u);
+}
+
+struct bb_ctx {
+  int device = 0;
+  int num_sms = 0;
+  size_t smem_optin = 0;
+  std::string last_error;
+  int64_t launches = 0;
+  std::mutex mu;
+  DegTables* tabs[BB_MAX_DEGREE + 2] = {};
+  double* d_red = nullptr;     // reduction scratch (FP64 partials)
+  size_t red_cap = 0;          // entries
+  double* h_red = nullptr;     // pinned host mirror
+};
+
+// Error helpers -----------------------------------------------------------------------
+int bb_fail(bb_ctx* ctx, int code, const char* fmt, ...);
+#define BB_CUDA(ctx, call)                                                        \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess)                                                        \
+      return bb_fail((ctx), BB_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+// Builds (or returns the cached) tables of degree N. Returns nullptr on failure.
+const DegTables* bb_tables(bb_ctx* ctx, int N);
+// Makes the context's device current.
+int bb_set_device(bb_ctx* ctx);
+// Checks a launch and counts it.
+int bb_check_launch(bb_ctx* ctx, const char* what);
+
+inline size_t dtype_size(int dtype) { return dtype == BB_F64 ? 8 : 4; }
+inline bool valid_dtype(int dtype) { return dtype == BB_F32 || dtype == BB_F64; }
+inline bool valid_degree(int N) { return N >= 1 && N <= BB_MAX_DEGREE; }
+
+// Shared-memory view of the degree tables, filled by load_tables().
+struct SmemTables {
+  const uint32_t* node3;
+  const uint32_t* node3m1;
+  const uint16_t* node2;
+  const uint16_t* fvol;
+  const uint16_t* fperm;
+};
+
+// Copies `words` 32-bit words of tables into shared memory (all threads participate).
+__device__ __forceinline__ SmemTables load_tables(const DegTables& t, const uint32_t* g,
+                                                  uint32_t* s) {
+  for (int w = threadIdx.x; w < t.nwords; w += blockDim.x) s[w] = __ldg(g + w);
+  SmemTables r;
+  r.node3 = s + t.o_node3;
+  r.node3m1 = s + t.o_node3m1;
+  r.node2 = reinterpret_cast<const uint16_t*>(s + t.o_node2);
+  r.fvol = reinterpret_cast<const uint16_t*>(s + t.o_fvol);
+  r.fperm = reinterpret_cast<const uint16_t*>(s + t.o_fperm);
+  return r;
+}
+
+template <class T>
+struct VecOf;
+template <>
+struct VecOf<float> {
+  using type = float4;
+  static constexpr int width = 4;
+};
+template <>
+struct VecOf<double> {
+  using type = double2;
+  static constexpr int width = 2;
+};
+
+// Block-cooperative copy of n elements global -> shared, 128-bit when both are aligned.
+template <class T>
+__device__ __forceinline__ void copy_g2s(T* __restrict__ s, const T* __restrict__ g, int n) {
+  using V = typename VecOf<T>::type;
+  constexpr int W = VecOf<T>::width;
+  if ((((uintptr_t)g | (uintptr_t)s) & 15) == 0) {
+    const int nv = n / W;
+    const V* gv = reinterpret_cast<const V*>(g);
+    V* sv = reinterpret_cast<V*>(s);
+    for (int t = threadIdx.x; t < nv; t += blockDim.x) sv[t] = __ldg(gv + t);
+    for (int t = nv * W + threadIdx.x; t < n; t += blockDim.x) s[t] = __ldg(g + t);
+  } else {
+    for (int t = threadIdx.x; t < n; t += blockDim.x) s[t] = __ldg(g + t);
+  }
+}
+
+// Block-cooperative copy shared -> global.
+template <class T>
+__device__ __forceinline__ void copy_s2g(T* __restrict__ g, const T* __restrict__ s, int n) {
+  using V = typename VecOf<T>::type;
+  constexpr int W = VecOf<T>::width;
+  if ((((uintptr_t)g | (uintptr_t)s) & 15) == 0) {
+    const int nv = n / W;
+    V* gv = reinterpret_cast<V*>(g);
+    const V* sv = reinterpret_cast<const V*>(s);
+    for (int t = threadIdx.x; t < nv; t += blockDim.x) gv[t] = sv[t];
+    for (int t = nv * W + threadIdx.x; t < n; t += blockDim.x) g[t] = s[t];
+  } else {
+    for (int t = threadIdx.x; t < n; t += blockDim.x) g[t] = s[t];
+  }
+}
+
+// Rounds a shared-memory byte offset up to 16 bytes.
+__host__ __device__ __forceinline__ size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+// One face's recursive lift, accumulated into a shared-memory volume block, for `ne`
+// elements and `nfld` fields at once (src/BernsteinLift.jl:139-164 applied per face and
+// summed through the permutations of :207-218):
+//   F = E_{N->N+1} x;  E0 = (N+1)^2/2 * R_{N+1} F;  layer 0 += E0;
+//   E_d = R_{N-d+1} E_{d-1};  layer d += l_d E_d   (d = 1..N)
+// Level-parallel: one thread per output coefficient, a block barrier between levels, and
+// two ping-pong buffers (the reference's in-place reduction is not parallel-safe).
+//   in(le, fld)  : Nfp face coefficients at in + (le*in_es + fld*in_fs)
+//   out(le, fld) : Np volume coefficients at out + (le*out_es + fld*out_fs)
+//   bufA/bufB    : ne*nfld*np2(N+1) scratch each
+// All threads of the block must call it.
+template <class T>
+__device__ void lift_face_accumulate(int N, int f, int ne, int nfld, const uint16_t* node2,
+                                     const T* in, int in_es, int in_fs, T* out, int out_es,
+                                     int out_fs, T* bufA, T* bufB, const T* lj) {
+  const int S = np2(N + 1);
+  const int nchain = ne * nfld;
+  // elevation, degree N -> N+1 (src/BernsteinLift.jl:100-125)
+  {
+    const int n = N + 1;
+    const int cnt = np2(n);
+    const uint16_t* dec = node2 + np3(n - 1);
+    const T inv = T(1) / T(n);
+    for (int it = threadIdx.x; it < nchain * cnt; it += blockDim.x) {
+      const int ch = it / cnt, m = it - ch * cnt;
+      const int le = ch / nfld, fld = ch - le * nfld;
+      const T* x = in + le * in_es + fld * in_fs;
+      const int a = dec[m] & 0xff, b = dec[m] >> 8, c = n - a - b;
+      T val = T(0);
+      if (a > 0) val = T(a) * x[ij2(N, a - 1, b)];
+      if (b > 0) val = fma(T(b), x[ij2(N, a, b - 1)], val);
+      if (c > 0) val = fma(T(c), x[ij2(N, a, b)], val);
+      bufA[ch * S + m] = val * inv;
+    }
+  }
+  __syncthreads();
+  // reduction chain: level 0 is the L0 apply (degree N+1 -> N, scaled by (N+1)^2/2)
+  T* src = bufA;
+  T* dst = bufB;
+  for (int d = 0; d <= N; ++d) {
+    const int n = N + 1 - d;         // input degree
+    const int cnt = np2(n - 1);      // outputs
+    const uint16_t* dec = node2 + np3(n - 2);
+    const T inv = T(1) / T(n);
+    const T scale = (d == 0) ? T((N + 1) * (N + 1)) / T(2) : T(1);
+    const T wl = (d == 0) ? T(1) : lj[d];
+    for (int it = threadIdx.x; it < nchain * cnt; it += blockDim.x) {
+      const int ch = it / cnt, m = it - ch * cnt;
+      const int le = ch / nfld, fld = ch - le * nfld;
+      const int a = dec[m] & 0xff, b = dec[m] >> 8;
+      const T* x = src + ch * S;
+      // reduction_multiply! (src/BernsteinLift.jl:81-85)
+      T val = fma(T(a + 1), x[ij2(n, a + 1, b)],
+                  fma(T(b + 1), x[ij2(n, a, b + 1)], T(n - a - b) * x[ij2(n, a, b)]));
+      val = (val * inv) * scale;
+      dst[ch * S + m] = val;
+      T* o = out + le * out_es + fld * out_fs;
+      o[face_vol(N, f, a, b, d)] += wl * val;
+    }
+    __syncthreads();
+    T* tmp = src;
+    src = dst;
+    dst = tmp;
+  }
+}

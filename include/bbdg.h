@@ -1,0 +1,146 @@
+/*
+ * bbdg.h -- C ABI of the GB300 (sm_103a) Bernstein DG hot path.
+ *
+ * Drop-in boundary for vincentxwang/BernsteinBasis.jl: the Julia operator types
+ * (BernsteinDerivativeMatrix_3D_{r,s,t}, BernsteinLift) keep their mul! API and dispatch to
+ * these entry points by ccall for device arrays; the examples' rhs_matvec! and time loop map
+ * onto the solver entry points. Every function returns a bb_status (0 = success) and never
+ * aborts; bb_ctx_last_error() describes the most recent failure on a context.
+ *
+ * Conventions
+ *   - Array arguments are DEVICE pointers owned by the caller unless a name ends in _host.
+ *   - Matrix operands keep the reference layout: one column per element, column-major,
+ *     i.e. element e's Np (or 4*Nfp) coefficients are contiguous at offset e*Np.
+ *   - Solver state is field-major structure-of-arrays: q[field][element][node], i.e. each
+ *     field is the reference's Np x K matrix; fields are (p,u,v,w) for the wave equation and
+ *     (Hx,Hy,Hz,Ex,Ey,Ez) for Maxwell, as in examples/3d_wave.jl and examples/3d_maxwell.jl.
+ *   - dtype selects FP32 (BB_F32) or FP64 (BB_F64) storage and arithmetic.
+ *   - Calls are ordered on the given cudaStream_t (passed as void*; NULL = legacy stream).
+ *   - A context holds scratch, tables and CUDA graphs; use one context per host thread.
+ */
+#ifndef BBDG_H
+#define BBDG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  BB_OK = 0,
+  BB_ERR_ARG = 1,       /* invalid argument (degree, size, null pointer, alignment, ...) */
+  BB_ERR_CUDA = 2,      /* a CUDA runtime call failed */
+  BB_ERR_TIMEOUT = 3,   /* a device-side bounded wait ran out */
+  BB_ERR_NONFINITE = 4, /* NaN or Inf detected by a checked reduction */
+  BB_ERR_STATE = 5,     /* call not valid in the object's current state */
+  BB_ERR_NOMEM = 6,     /* device or host allocation failed */
+  BB_ERR_DEVICE = 7     /* device-side check failed (corrupt connectivity, bad index) */
+} bb_status;
+
+typedef enum { BB_F32 = 0, BB_F64 = 1 } bb_dtype;
+typedef enum { BB_WAVE = 0, BB_MAXWELL = 1 } bb_physics;
+typedef enum { BB_AXIS_R = 0, BB_AXIS_S = 1, BB_AXIS_T = 2 } bb_axis;
+
+#define BB_MAX_DEGREE 20
+/* Per-element geometry record (bb_solver_create): rxJ sxJ txJ ryJ syJ tyJ rzJ szJ tzJ,
+ * 1/J, J, (unused), nxJ[4], nyJ[4], nzJ[4] -- StartUpDG's md fields for affine tets. */
+#define BB_GEO_STRIDE 24
+
+typedef struct bb_ctx bb_ctx;
+typedef struct bb_solver bb_solver;
+
+/* ---- context ------------------------------------------------------------------------ */
+int bb_version(void);
+int bb_ctx_create(int device, bb_ctx** out);
+int bb_ctx_destroy(bb_ctx* ctx);
+const char* bb_ctx_last_error(const bb_ctx* ctx);
+/* Number of kernels this context has launched (for launch accounting). */
+int64_t bb_ctx_launch_count(const bb_ctx* ctx);
+
+/* ---- reference-element operators, matrix form (one column per element) -------------- */
+
+/* out = D x for D in {Dr, Ds, Dt} (axis 0/1/2).
+ * Replaces LinearAlgebra.mul!(out, D::BernsteinDerivativeMatrix_3D_{r,s,t}, x::Matrix),
+ * src/BernsteinDerivativeMatrix_3D.jl:222-231 (vector form :134,:176,:218 is K = 1). */
+int bb_deriv_apply(bb_ctx* ctx, int axis, int N, int64_t K, int dtype, const void* x,
+                   void* out, void* stream);
+
+/* dr, ds, dt = Dr x, Ds x, Dt x from one read of x (fused form of the three calls above). */
+int bb_grad_apply(bb_ctx* ctx, int N, int64_t K, int dtype, const void* x, void* dr,
+                  void* ds, void* dt, void* stream);
+
+/* out = L x with L the Bernstein lift [L1|L2|L3|L4]; x holds 4*Nfp face coefficients per
+ * element (faces s=-1, r+s+t=-1, r=-1, t=-1).
+ * Replaces LinearAlgebra.mul!(out, L::BernsteinLift, x), src/BernsteinLift.jl:191-220 and
+ * the matrix form :264-269. */
+int bb_lift_apply(bb_ctx* ctx, int N, int64_t K, int dtype, const void* faces, void* out,
+                  void* stream);
+
+/* Single-face lift (Nfp -> Np per column). Replaces face_lift_multiply!,
+ * src/BernsteinLift.jl:139-164 and its matrix form :174-179. */
+int bb_face_lift_apply(bb_ctx* ctx, int N, int64_t K, int dtype, const void* x, void* out,
+                       void* stream);
+
+/* 2D degree elevation N -> N+1 and reduction N -> N-1, one column per face.
+ * Replace elevation_multiply! (src/BernsteinLift.jl:100-125) and reduction_multiply!
+ * (src/BernsteinLift.jl:66-90). */
+int bb_elevation_apply(bb_ctx* ctx, int N, int64_t K, int dtype, const void* x, void* out,
+                       void* stream);
+int bb_reduction_apply(bb_ctx* ctx, int N, int64_t K, int dtype, const void* x, void* out,
+                       void* stream);
+
+/* Fused operator pass: dr, ds, dt = D{r,s,t} x and lift = L faces in one launch. */
+int bb_fused_apply(bb_ctx* ctx, int N, int64_t K, int dtype, const void* x,
+                   const void* faces, void* dr, void* ds, void* dt, void* lift, void* stream);
+
+/* ---- DG solver (examples/3d_wave.jl, examples/3d_maxwell.jl) ------------------------- */
+
+/* conn: K*4 int32, conn[e*4+f] = nbr << 5 | nbr_face << 3 | orientation (device).
+ * geo:  K*BB_GEO_STRIDE values of the solver dtype (device).
+ * tau <= 0: the examples' interface flux exactly as written; tau > 0: the same upwind
+ * flux with its penalty scaled by the face Jacobian |nJ| (stable at dt ~ h/(N+1)^2).
+ * Both arrays must stay alive and unchanged while the solver exists. */
+int bb_solver_create(bb_ctx* ctx, int physics, int N, int64_t K, int dtype,
+                     const int32_t* conn, const void* geo, double tau, bb_solver** out);
+int bb_solver_destroy(bb_solver* s);
+/* Elements per thread block and threads per block of the stage kernels (0 = default). */
+int bb_solver_set_tile(bb_solver* s, int elems_per_block, int threads);
+int bb_solver_get_tile(const bb_solver* s, int* elems_per_block, int* threads);
+
+/* rhs = RHS(q): one evaluation of rhs_matvec! (examples/3d_wave.jl:36-84,
+ * examples/3d_maxwell.jl:36-93). */
+int bb_rhs(bb_solver* s, const void* q, void* rhs, void* stream);
+
+/* nsteps steps of 5-stage 4th-order low-storage Runge-Kutta, q and res updated in place.
+ * res must start at zero or hold the previous step's residual (its first stage ignores it).
+ * use_graph != 0 replays each step from a CUDA graph. */
+int bb_lsrk_run(bb_solver* s, double dt, int nsteps, void* q, void* res, int use_graph,
+                void* stream);
+
+/* The same with host state: copies q_host_in to q_dev, advances, copies back to
+ * q_host_out (pinned host memory recommended). */
+int bb_lsrk_run_host(bb_solver* s, double dt, int nsteps, const void* q_host_in,
+                     void* q_host_out, void* q_dev, void* res_dev, int use_graph,
+                     void* stream);
+
+/* ---- reductions (FP64 accumulation, warp-shuffle trees) ------------------------------ */
+
+/* For each field f of nf fields laid out as [nf][K][Np]:
+ *   out_host[3f+0] = sum a^2, out_host[3f+1] = sum (a-b)^2, out_host[3f+2] = sum b^2
+ * (b may be NULL: then the last two are 0). Returns BB_ERR_NONFINITE if any sum is not
+ * finite. Synchronises the stream. */
+int bb_norms(bb_ctx* ctx, int N, int64_t K, int nf, int dtype, const void* a, const void* b,
+             double* out_host, void* stream);
+
+/* Mass-matrix energy: out_host[f] = sum_e J_e (a_e^T M a_e) with M the Bernstein mass
+ * matrix of the reference tetrahedron; with b != NULL the quadratic form of (a - b).
+ * J is read from the geometry records (stride BB_GEO_STRIDE, solver dtype). */
+int bb_mass_norms(bb_ctx* ctx, int N, int64_t K, int nf, int dtype, const void* a,
+                  const void* b, const void* geo, double* out_host, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BBDG_H */

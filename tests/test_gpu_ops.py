@@ -1,0 +1,145 @@
+"""GPU parity of the reference-element operators (through the C ABI) vs the CPU oracle.
+
+Tolerances (relative l2 over each output): FP64 1e-12, FP32 1e-5.
+"""
+import ctypes
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"f64": 1e-12, "f32": 1e-5}
+DEGREES = [1, 2, 3, 4, 5, 7, 9, 10, 12, 15]
+
+
+def rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def torch_dtype(name):
+    import torch
+    return torch.float64 if name == "f64" else torch.float32
+
+
+@pytest.mark.parametrize("dt", ["f64", "f32"])
+@pytest.mark.parametrize("N", DEGREES)
+def test_derivative_matches_oracle(cuda, bb, oracle_cpu, N, dt):
+    import torch
+    rng = np.random.default_rng(N)
+    K, Np = 37, bb.np3(N)
+    x = rng.uniform(-1, 1, (K, Np))
+    xd = torch.tensor(x, dtype=torch_dtype(dt), device=cuda)
+    outs = [torch.empty_like(xd) for _ in range(3)]
+    for axis, D in enumerate((bb.BernsteinDerivativeMatrix_3D_r(N), bb.BernsteinDerivativeMatrix_3D_s(N),
+                              bb.BernsteinDerivativeMatrix_3D_t(N))):
+        bb.mul_(outs[axis], D, xd)
+        want = oracle_cpu.deriv(axis, N, x)
+        assert rel(outs[axis].cpu().numpy(), want) < TOL[dt], (N, axis)
+    g = [torch.empty_like(xd) for _ in range(3)]
+    bb.grad_(g[0], g[1], g[2], N, xd)
+    for a in range(3):
+        assert torch.equal(g[a], outs[a])
+
+
+@pytest.mark.parametrize("dt", ["f64", "f32"])
+@pytest.mark.parametrize("N", DEGREES)
+def test_lift_matches_oracle(cuda, bb, oracle_cpu, N, dt):
+    import torch
+    rng = np.random.default_rng(50 + N)
+    K, Np, Nfp = 29, bb.np3(N), bb.np2(N)
+    x = rng.uniform(-1, 1, (K, 4 * Nfp))
+    xd = torch.tensor(x, dtype=torch_dtype(dt), device=cuda)
+    out = torch.empty((K, Np), dtype=xd.dtype, device=cuda)
+    bb.mul_(out, bb.BernsteinLift(N), xd)
+    assert rel(out.cpu().numpy(), oracle_cpu.lift(N, x)) < TOL[dt]
+    # single face (face_lift_multiply!)
+    xf = torch.tensor(x[:, :Nfp].copy(), dtype=xd.dtype, device=cuda)
+    of = torch.empty((K, Np), dtype=xd.dtype, device=cuda)
+    bb.face_lift_multiply_(of, bb.BernsteinLift(N), xf)
+    want = np.stack([oracle_cpu.face_lift(N, x[e, :Nfp]) for e in range(K)])
+    assert rel(of.cpu().numpy(), want) < TOL[dt]
+
+
+@pytest.mark.parametrize("dt", ["f64", "f32"])
+@pytest.mark.parametrize("N", [1, 2, 5, 9, 14, 19])
+def test_elevation_reduction_match_oracle(cuda, bb, oracle_cpu, N, dt):
+    import torch
+    rng = np.random.default_rng(70 + N)
+    K = 11
+    x = rng.uniform(-1, 1, (K, bb.np2(N)))
+    xd = torch.tensor(x, dtype=torch_dtype(dt), device=cuda)
+    up = torch.empty((K, bb.np2(N + 1)), dtype=xd.dtype, device=cuda)
+    dn = torch.empty((K, bb.np2(N - 1)), dtype=xd.dtype, device=cuda)
+    bb.elevation_multiply_(up, N, xd)
+    bb.reduction_multiply_(dn, N, xd)
+    assert rel(up.cpu().numpy(), np.stack([oracle_cpu.elevation(N, r) for r in x])) < TOL[dt]
+    assert rel(dn.cpu().numpy(), np.stack([oracle_cpu.reduction(N, r) for r in x])) < TOL[dt]
+
+
+@pytest.mark.parametrize("N", [3, 9])
+def test_fused_operator_pass(cuda, bb, N):
+    import torch
+    rng = np.random.default_rng(90 + N)
+    K = 23
+    x = torch.tensor(rng.uniform(-1, 1, (K, bb.np3(N))), device=cuda)
+    f = torch.tensor(rng.uniform(-1, 1, (K, 4 * bb.np2(N))), device=cuda)
+    dr, ds, dt_, li = (torch.empty_like(x) for _ in range(4))
+    bb.fused_apply_(dr, ds, dt_, li, N, x, f)
+    ref = [torch.empty_like(x) for _ in range(4)]
+    bb.grad_(ref[0], ref[1], ref[2], N, x)
+    bb.mul_(ref[3], bb.BernsteinLift(N), f)
+    for a, b in zip((dr, ds, dt_, li), ref):
+        assert torch.equal(a, b)
+
+
+def _golden():
+    path = os.path.join(os.path.dirname(__file__), "golden", "operators_exact.json")
+    with open(path) as fh:
+        return json.load(fh)["cases"]
+
+
+@pytest.mark.parametrize("case", _golden(), ids=lambda c: f"{c['op']}-N{c['N']}")
+def test_gpu_matches_exact_golden(cuda, bb, case):
+    import torch
+    N = case["N"]
+    x = torch.tensor(case["x"]["float"], dtype=torch.float64, device=cuda)
+    y = np.array(case["y"]["float"])
+    out = torch.empty(len(y), dtype=torch.float64, device=cuda)
+    op = case["op"]
+    if op[0] == "D":
+        D = getattr(bb, f"BernsteinDerivativeMatrix_3D_{op[1]}")(N)
+        bb.mul_(out, D, x)
+    elif op == "elevation":
+        bb.elevation_multiply_(out, N, x)
+    elif op == "reduction":
+        bb.reduction_multiply_(out, N, x)
+    elif op == "face_lift":
+        bb.face_lift_multiply_(out, bb.BernsteinLift(N), x)
+    else:
+        bb.mul_(out, bb.BernsteinLift(N), x)
+    assert rel(out.cpu().numpy(), y) < 1e-13
+
+
+def test_bad_arguments_return_status(cuda, bb):
+    import torch
+    from bbdg import _lib
+    from bbdg.context import get_context
+    L = _lib.load()
+    ctx = get_context(0)
+    x = torch.zeros(20, dtype=torch.float64, device=cuda)
+    p = ctypes.c_void_p(x.data_ptr())
+    assert L.bb_deriv_apply(ctx.handle, 0, 0, 1, 1, p, p, None) == _lib.BB_ERR_ARG
+    assert L.bb_deriv_apply(ctx.handle, 0, 21, 1, 1, p, p, None) == _lib.BB_ERR_ARG
+    assert L.bb_deriv_apply(ctx.handle, 3, 3, 1, 1, p, p, None) == _lib.BB_ERR_ARG
+    assert L.bb_deriv_apply(ctx.handle, 0, 3, 1, 7, p, p, None) == _lib.BB_ERR_ARG
+    assert L.bb_lift_apply(ctx.handle, 3, 1, 1, None, p, None) == _lib.BB_ERR_ARG
+    with pytest.raises(ValueError):
+        bb.mul_(torch.empty(20, device=cuda, dtype=torch.float64), bb.BernsteinDerivativeMatrix_3D_r(3),
+                torch.empty(21, device=cuda, dtype=torch.float64))
+    with pytest.raises(ValueError):
+        bb.mul_(torch.empty(20, dtype=torch.float64), bb.BernsteinDerivativeMatrix_3D_r(3),
+                torch.empty(20, dtype=torch.float64))

@@ -1,0 +1,165 @@
+"""GPU parity of the fused DG right-hand side and LSRK stepping vs the CPU oracle.
+
+The oracle restates examples/3d_wave.jl:36-84 and examples/3d_maxwell.jl:36-93 loop for
+loop (AoS SVector layout, Fmask/mapP gather, 9 derivative applies, BernsteinLift mul!).
+Tolerances, relative l2 per field: FP64 1e-12, FP32 1e-5 (FP32 is checked against the
+FP64 oracle).
+"""
+import numpy as np
+import pytest
+
+from oracle import meshdata
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"f64": 1e-12, "f32": 1e-5}
+
+
+def per_field_rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return np.array([np.linalg.norm(a[f] - b[f]) / max(np.linalg.norm(b[f]), 1e-300)
+                     for f in range(a.shape[0])])
+
+
+def tdt(name):
+    import torch
+    return torch.float64 if name == "f64" else torch.float32
+
+
+def random_state(rng, nf, K, Np):
+    return rng.uniform(-1, 1, (nf, K, Np))
+
+
+@pytest.mark.parametrize("dt", ["f64", "f32"])
+@pytest.mark.parametrize("tau", [0.0, 1.0])
+@pytest.mark.parametrize("physics", ["wave", "maxwell"])
+@pytest.mark.parametrize("N", [1, 2, 3, 5, 7, 9])
+def test_rhs_matches_oracle(cuda, bb, oracle_cpu, N, physics, tau, dt):
+    import torch
+    m = bb.uniform_tet_mesh(3)
+    md = meshdata.build(m, N)
+    s = bb.DGSolver(m, N, physics, dtype=tdt(dt), tau=tau)
+    rng = np.random.default_rng(N * 7 + len(physics))
+    q = random_state(rng, s.nf, m.K, s.Np)
+    qd = torch.tensor(q, dtype=tdt(dt), device=cuda)
+    got = s.rhs(qd).cpu().numpy()
+    want = oracle_cpu.rhs(0 if physics == "wave" else 1, N, q, md, tau=tau)
+    err = per_field_rel(got, want)
+    assert np.all(err < TOL[dt]), err
+
+
+@pytest.mark.parametrize("epb", [1, 2, 4, 5, 6, 12, 18])
+def test_tiling_does_not_change_results(cuda, bb, epb):
+    import torch
+    m = bb.uniform_tet_mesh(3)
+    N = 4
+    s = bb.DGSolver(m, N, "maxwell", dtype=torch.float64, tau=1.0)
+    rng = np.random.default_rng(5)
+    q0 = torch.tensor(random_state(rng, 6, m.K, s.Np), device=cuda)
+    ref_rhs = s.rhs(q0)
+    q_ref, r_ref = q0.clone(), torch.zeros_like(q0)
+    s.run(q_ref, r_ref, 1e-3, 3, graph=False)
+    s.set_tile(epb)
+    assert s.tile[0] == epb
+    assert torch.equal(s.rhs(q0), ref_rhs)
+    q, r = q0.clone(), torch.zeros_like(q0)
+    s.run(q, r, 1e-3, 3, graph=False)
+    assert torch.equal(q, q_ref) and torch.equal(r, r_ref)
+
+
+@pytest.mark.parametrize("dt", ["f64", "f32"])
+@pytest.mark.parametrize("physics", ["wave", "maxwell"])
+@pytest.mark.parametrize("N", [2, 4, 6])
+def test_lsrk_matches_oracle(cuda, bb, oracle_cpu, N, physics, dt):
+    import torch
+    m = bb.uniform_tet_mesh(3)
+    md = meshdata.build(m, N)
+    s = bb.DGSolver(m, N, physics, dtype=tdt(dt), tau=1.0)
+    f = bb.gaussian_pulses(seed=N)
+    zero = lambda x, y, z: 0 * x
+    fields = [f] + [zero] * (s.nf - 1) if physics == "wave" else [zero] * 5 + [f]
+    q0 = bb.project_fields(m, N, fields)
+    step = s.dt_cfl()
+    nsteps = 5
+    qd = torch.tensor(q0, dtype=tdt(dt), device=cuda)
+    rd = torch.zeros_like(qd)
+    s.run(qd, rd, step, nsteps, graph=True)
+    q_or, r_or = oracle_cpu.lsrk(0 if physics == "wave" else 1, N, q0, md, step, nsteps, tau=1.0)
+    err = per_field_rel(qd.cpu().numpy(), q_or)
+    nz = [i for i in range(s.nf) if np.linalg.norm(q_or[i]) > 0]
+    assert np.all(err[nz] < TOL[dt]), err
+
+
+def test_graph_and_stream_paths_agree(cuda, bb):
+    import torch
+    m = bb.uniform_tet_mesh(3)
+    N = 5
+    s = bb.DGSolver(m, N, "wave", dtype=torch.float32, tau=1.0)
+    q0 = s.project([bb.gaussian_pulses(1), lambda x, y, z: 0 * x, lambda x, y, z: 0 * x,
+                    lambda x, y, z: 0 * x])
+    qa, ra = q0.clone(), torch.zeros_like(q0)
+    qb, rb = q0.clone(), torch.zeros_like(q0)
+    s.run(qa, ra, s.dt_cfl(), 7, graph=False)
+    s.run(qb, rb, s.dt_cfl(), 4, graph=True)
+    s.run(qb, rb, s.dt_cfl(), 3, graph=True)
+    torch.cuda.synchronize()
+    assert torch.equal(qa, qb)
+    # host-buffer path (copies inside the call) gives the same state
+    hin = q0.cpu().pin_memory()
+    hout = torch.empty_like(hin).pin_memory()
+    qd, rd = torch.empty_like(q0), torch.zeros_like(q0)
+    s.run_host(hin, hout, qd, rd, s.dt_cfl(), 7)
+    torch.cuda.synchronize()
+    assert torch.equal(hout, qa.cpu())
+
+
+def test_config1_anchor_fp64_and_fp32(cuda, bb, oracle_cpu):
+    """Wave, N=7, 4^3 hexes x 6 tets (K=384), p0 = exp(-10 r^2), 100 LSRK45 steps,
+    dt = 0.25 h/(N+1)^2: FP64 GPU within 1e-12 and FP32 GPU within 1e-5 of the FP64 oracle."""
+    import torch
+    m = bb.uniform_tet_mesh(4)
+    N = 7
+    md = meshdata.build(m, N)
+    zero = lambda x, y, z: 0 * x
+    q0 = bb.project_fields(m, N, [lambda x, y, z: np.exp(-10 * (x * x + y * y + z * z)),
+                                  zero, zero, zero])
+    dt = 0.25 * 0.5 / (N + 1) ** 2
+    q_or, _ = oracle_cpu.lsrk(0, N, q0, md, dt, 100, tau=1.0)
+    for name in ("f64", "f32"):
+        s = bb.DGSolver(m, N, "wave", dtype=tdt(name), tau=1.0)
+        qd = torch.tensor(q0, dtype=tdt(name), device=cuda)
+        rd = torch.zeros_like(qd)
+        s.run(qd, rd, dt, 100)
+        err = per_field_rel(qd.cpu().numpy(), q_or)
+        assert np.all(err < TOL[name]), (name, err)
+
+
+def test_norms_and_mass_energy(cuda, bb):
+    import torch
+    from oracle import dense
+    m = bb.uniform_tet_mesh(2)
+    N = 3
+    s = bb.DGSolver(m, N, "wave", dtype=torch.float64, tau=1.0)
+    rng = np.random.default_rng(11)
+    a = rng.standard_normal((4, m.K, s.Np))
+    b = rng.standard_normal((4, m.K, s.Np))
+    A, B = torch.tensor(a, device=cuda), torch.tensor(b, device=cuda)
+    nrm = s.norms(A, B)
+    assert np.allclose(nrm[:, 0], (a ** 2).sum(axis=(1, 2)), rtol=1e-12)
+    assert np.allclose(nrm[:, 1], ((a - b) ** 2).sum(axis=(1, 2)), rtol=1e-12)
+    assert np.allclose(nrm[:, 2], (b ** 2).sum(axis=(1, 2)), rtol=1e-12)
+    M = np.array(dense.mass(N))
+    want = np.einsum("fkn,nm,fkm,k->f", a - b, M, a - b, m.J)
+    assert np.allclose(s.mass_norms(A, B), want, rtol=1e-11)
+
+
+def test_corrupt_connectivity_is_reported(cuda, bb):
+    import torch
+    from bbdg import BBError
+    m = bb.uniform_tet_mesh(2)
+    m.conn = m.conn.copy()
+    m.conn[3, 1] = np.int32((m.K + 5) << 5)   # neighbour index out of range
+    s = bb.DGSolver(m, 2, "wave", dtype=torch.float64, tau=1.0)
+    with pytest.raises(BBError) as ei:
+        s.rhs(s.zeros())
+    assert ei.value.status == 7

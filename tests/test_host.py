@@ -1,0 +1,111 @@
+"""Host-side logic (no GPU): mesh, compact connectivity vs coordinate-matched mapP,
+geometric factors, projection, and the C-ABI library's exported symbols."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import meshdata
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "bbdg.h")).read()
+    return re.findall(r"^\s*(?:int|int64_t|const char\*)\s+(bb_\w+)\(", src, re.M)
+
+
+def test_capi_library_exports_every_declared_symbol():
+    from bbdg import _lib, _build
+    path = _build.build()
+    lib = ctypes.CDLL(path)
+    names = header_functions()
+    assert len(names) >= 20
+    for name in names:
+        assert hasattr(lib, name), name
+    # the Python binding covers the same set
+    assert set(names) <= set(_lib.SIGNATURES), set(names) - set(_lib.SIGNATURES)
+
+
+def neighbour_node(N, o, a_idx):
+    """Face node a of this side -> node index on the partner side (orientation o)."""
+    from bbdg.mesh import PERMS
+    pairs = [(a, b) for b in range(N + 1) for a in range(N + 1 - b)]
+    a, b = pairs[a_idx]
+    w = (a, b, N - a - b)
+    wn = [0, 0, 0]
+    for v in range(3):
+        wn[PERMS[o][v]] = w[v]
+    return pairs.index((wn[0], wn[1]))
+
+
+@pytest.mark.parametrize("n,N", [(2, 1), (2, 3), (3, 2), (4, 4)])
+def test_compact_connectivity_matches_mapP(bb, n, N):
+    m = bb.uniform_tet_mesh(n)
+    md = meshdata.build(m, N)
+    Nfp = (N + 1) * (N + 2) // 2
+    table = [[neighbour_node(N, o, a) for a in range(Nfp)] for o in range(6)]
+    conn = m.conn.astype(np.int64)
+    nbr, nface, orient = conn >> 5, (conn >> 3) & 3, conn & 7
+    for e in range(m.K):
+        for f in range(4):
+            for a in range(Nfp):
+                want = md.mapP[(e * 4 + f) * Nfp + a]
+                got = (nbr[e, f] * 4 + nface[e, f]) * Nfp + table[orient[e, f]][a]
+                assert got == want
+
+
+def test_mesh_periodic_pairs_and_volume(bb):
+    m = bb.uniform_tet_mesh(3)
+    assert m.K == 6 * 27
+    # pairing is an involution and never pairs a face with itself
+    for e in range(m.K):
+        for f in range(4):
+            e2, f2 = m.nbr[e, f], m.nbr_face[e, f]
+            assert (e2, f2) != (e, f)
+            assert m.nbr[e2, f2] == e and m.nbr_face[e2, f2] == f
+    vol = (4.0 / 3.0) * m.J.sum()
+    assert vol == pytest.approx(8.0, rel=1e-13)
+
+
+def test_geometry_matches_oracle_meshdata(bb):
+    m = bb.uniform_tet_mesh(3)
+    N = 2
+    md = meshdata.build(m, N)
+    from bbdg.mesh import GEO_NX, GEO_NY, GEO_NZ, GEO_INVJ, GEO_J
+    assert np.allclose(m.geo[:, :9], md.geo9, rtol=1e-14, atol=1e-15)
+    assert np.allclose(m.geo[:, GEO_J], md.Jall)
+    assert np.allclose(m.geo[:, GEO_INVJ], 1 / md.Jall)
+    Nfp = (N + 1) * (N + 2) // 2
+    for f in range(4):
+        for c, base in enumerate((GEO_NX, GEO_NY, GEO_NZ)):
+            assert np.allclose(m.geo[:, base + f], md.nJ[:, f * Nfp, c], atol=1e-15)
+
+
+@pytest.mark.parametrize("N", [1, 3, 6])
+def test_projection_reproduces_polynomials(bb, N):
+    m = bb.uniform_tet_mesh(2)
+    f = lambda x, y, z: (1 + x + 2 * y - z) ** N
+    q = bb.project_fields(m, N, [f])[0]
+    # evaluate the Bernstein expansion at random points of every element
+    rng = np.random.default_rng(N)
+    lam = rng.dirichlet(np.ones(4), size=7)             # weights on lambda0..lambda3
+    from oracle.dense import vandermonde_tet
+    V, _ = vandermonde_tet(N, *lam.T)
+    u = q @ V.T                                          # (K, 7)
+    W = lam[:, [3, 0, 1, 2]]                             # weights on X1..X4
+    X = np.einsum("pm,kmc->kpc", W, m.EVX)
+    assert np.allclose(u, f(X[..., 0], X[..., 1], X[..., 2]), rtol=1e-9, atol=1e-9)
+
+
+def test_face_node_tables_agree_with_oracle_fmask(bb):
+    for N in range(1, 10):
+        fv = bb.ordering.face_node_volume_index(N).reshape(-1)
+        assert np.array_equal(fv, meshdata.fmask(N))
+
+
+def test_product_rejects_bad_degree(bb):
+    with pytest.raises(ValueError):
+        bb.mesh.uniform_tet_mesh(1)
