@@ -52,6 +52,8 @@ SIGNATURES = {
     "bb_solver_destroy": (_I, [_P]),
     "bb_solver_set_tile": (_I, [_P, _I, _I]),
     "bb_solver_get_tile": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    "bb_solver_set_kernel": (_I, [_P, _I]),
+    "bb_solver_get_kernel": (_I, [_P]),
     "bb_rhs": (_I, [_P, _P, _P, _P]),
     "bb_lsrk_run": (_I, [_P, _D, _I, _P, _P, _I, _P]),
     "bb_lsrk_run_host": (_I, [_P, _D, _I, _P, _P, _P, _P, _I, _P]),

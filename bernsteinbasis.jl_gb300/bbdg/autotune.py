@@ -1,0 +1,95 @@
+"""Per-degree tile autotuner for the stage kernels.
+
+For a solver it times every compiled tile variant (elements per block x threads per
+block; degree-specialised FP32 variants and the generic kernel) over a few LSRK steps on the
+solver's own mesh with CUDA events, keeps the fastest, and caches the choice per
+(physics, N, dtype, device name) in a JSON file next to the built library.
+"""
+from __future__ import annotations
+
+import json
+import os
+
+import torch
+
+from . import _build
+
+CACHE = os.path.join(_build.BUILD, "autotune.json")
+
+# Candidates (kernel, elements per block, threads per block).
+CANDIDATES = {
+    ("wave", 9, torch.float32): [("specialised", 4, 128), ("specialised", 4, 256),
+                                 ("specialised", 2, 64), ("specialised", 6, 192),
+                                 ("generic", 4, 256), ("generic", 2, 256)],
+    ("maxwell", 9, torch.float32): [("specialised", 2, 128), ("specialised", 2, 256),
+                                    ("generic", 2, 256), ("generic", 4, 256)],
+}
+GENERIC = [("generic", e, 256) for e in (1, 2, 4, 6, 12)]
+
+
+def _key(solver) -> str:
+    name = torch.cuda.get_device_name(solver.device)
+    return f"{solver.physics}|{solver.N}|{str(solver.dtype)}|{name}"
+
+
+def _load():
+    try:
+        with open(CACHE) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return {}
+
+
+def candidates(solver):
+    return CANDIDATES.get((solver.physics, solver.N, solver.dtype), GENERIC)
+
+
+def tune(solver, steps: int = 3, use_cache: bool = True, verbose: bool = False):
+    """Selects the fastest tile for `solver` (in place) and returns (epb, threads, table)."""
+    key = _key(solver)
+    cache = _load() if use_cache else {}
+    if key in cache:
+        kind, epb, nt = cache[key]["choice"]
+        solver.set_kernel(kind)
+        solver.set_tile(epb, nt)
+        return (kind, epb, nt), cache[key]["ms_per_step"]
+    q = (torch.rand((solver.nf, solver.K, solver.Np), dtype=solver.dtype,
+                    device=solver.device) - 0.5) * 1e-3
+    r = torch.zeros_like(q)
+    dt = solver.dt_cfl()
+    table = {}
+    for kind, epb, nt in candidates(solver):
+        try:
+            solver.set_kernel(kind)
+            solver.set_tile(epb, nt)
+        except Exception:
+            continue
+        if solver.kernel != kind:
+            continue
+        solver.run(q, r, dt, 1)
+        s0 = torch.cuda.Event(enable_timing=True)
+        s1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        s0.record()
+        solver.run(q, r, dt, steps)
+        s1.record()
+        torch.cuda.synchronize()
+        name = f"{kind}:{epb}x{nt}"
+        table[name] = s0.elapsed_time(s1) / steps
+        if verbose:
+            print(f"autotune {solver.physics} N={solver.N} {name}: {table[name]:.3f} ms/step")
+    if not table:
+        raise RuntimeError("no tile variant could run")
+    best = min(table, key=table.get)
+    kind, tile = best.split(":")
+    epb, nt = (int(v) for v in tile.split("x"))
+    solver.set_kernel(kind)
+    solver.set_tile(epb, nt)
+    cache[key] = {"choice": [kind, epb, nt], "ms_per_step": table}
+    try:
+        os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+        with open(CACHE, "w") as fh:
+            json.dump(cache, fh, indent=1)
+    except OSError:
+        pass
+    return (kind, epb, nt), table

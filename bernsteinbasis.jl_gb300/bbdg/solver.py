@@ -80,6 +80,17 @@ class DGSolver:
         self.ctx.check(_lib.load().bb_solver_set_tile(self.handle, int(elems_per_block),
                                                       int(threads)), "bb_solver_set_tile")
 
+    def set_kernel(self, kind: str) -> None:
+        """'specialised' (default: degree-specialised kernel when one exists) or 'generic'."""
+        if kind not in ("specialised", "generic"):
+            raise ValueError("kind must be 'specialised' or 'generic'")
+        self.ctx.check(_lib.load().bb_solver_set_kernel(self.handle, int(kind == "generic")),
+                       "bb_solver_set_kernel")
+
+    @property
+    def kernel(self) -> str:
+        return "specialised" if _lib.load().bb_solver_get_kernel(self.handle) == 0 else "generic"
+
     @property
     def tile(self):
         e, t = ctypes.c_int(), ctypes.c_int()

@@ -17,6 +17,7 @@
 #include <cstring>
 
 #include "bbdg_internal.cuh"
+#include "bbdg_stage_fast.cuh"
 
 namespace {
 
@@ -194,33 +195,36 @@ __global__ void __launch_bounds__(kThreads) stage_kernel(StageParams<T> P, TileL
       const int idx[4] = {ijk3(N, i + 1, j, k), ijk3(N, i, j + 1, k), ijk3(N, i, j, k + 1),
                           ijk3(N, i, j, k)};
       const T* g = sGeo + le * BB_GEO_STRIDE;
-      // barycentric weights of d/dx, d/dy, d/dz (times J): g_a = (rxJ, sxJ, txJ, -sum)/2
-      T gx[4], gy[4], gz[4];
+      // barycentric weights of d/dx, d/dy, d/dz (times J): g_a = (rxJ, sxJ, txJ, -sum)/2;
+      // the fourth weight is implied by the differences below
+      T gx[3], gy[3], gz[3];
       gx[0] = T(0.5) * g[0]; gx[1] = T(0.5) * g[1]; gx[2] = T(0.5) * g[2];
       gy[0] = T(0.5) * g[3]; gy[1] = T(0.5) * g[4]; gy[2] = T(0.5) * g[5];
       gz[0] = T(0.5) * g[6]; gz[1] = T(0.5) * g[7]; gz[2] = T(0.5) * g[8];
-      gx[3] = -(gx[0] + gx[1] + gx[2]);
-      gy[3] = -(gy[0] + gy[1] + gy[2]);
-      gz[3] = -(gz[0] + gz[1] + gz[2]);
       const T* q0 = sQ + (size_t)le * Np;
       auto F = [&](int fld, int a) { return q0[(size_t)fld * epb * Np + idx[a]]; };
       T w[NW];
 #pragma unroll
       for (int m = 0; m < NW; ++m) w[m] = T(0);
+      // sum_a g_a x(beta+e_a) with sum_a g_a = 0, formed as sum_{a<3} g_a (x_a - x_3) so
+      // that smooth data cancels in the differences (as the reference's Dr = (D0 - D3)/2)
       if constexpr (PHYS == BB_WAVE) {
+        const T p3 = F(0, 3), u3 = F(1, 3), v3 = F(2, 3), w3 = F(3, 3);
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          const T p = F(0, a), u = F(1, a), v = F(2, a), ww = F(3, a);
+        for (int a = 0; a < 3; ++a) {
+          const T p = F(0, a) - p3, u = F(1, a) - u3, v = F(2, a) - v3, ww = F(3, a) - w3;
           w[0] += gx[a] * u + gy[a] * v + gz[a] * ww;
           w[1] += gx[a] * p;
           w[2] += gy[a] * p;
           w[3] += gz[a] * p;
         }
       } else {
+        const T Hx3 = F(0, 3), Hy3 = F(1, 3), Hz3 = F(2, 3);
+        const T Ex3 = F(3, 3), Ey3 = F(4, 3), Ez3 = F(5, 3);
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          const T Hx = F(0, a), Hy = F(1, a), Hz = F(2, a);
-          const T Ex = F(3, a), Ey = F(4, a), Ez = F(5, a);
+        for (int a = 0; a < 3; ++a) {
+          const T Hx = F(0, a) - Hx3, Hy = F(1, a) - Hy3, Hz = F(2, a) - Hz3;
+          const T Ex = F(3, a) - Ex3, Ey = F(4, a) - Ey3, Ez = F(5, a) - Ez3;
           w[0] += -gy[a] * Ez + gz[a] * Ey;  // d/dt Hx = -dEz/dy + dEy/dz
           w[1] += gx[a] * Ez - gz[a] * Ex;   // d/dt Hy
           w[2] += -gx[a] * Ey + gy[a] * Ex;  // d/dt Hz
@@ -367,6 +371,8 @@ struct bb_solver {
   double tau = 0.0;
   const DegTables* tab = nullptr;
   int epb = 0, threads = kThreads;
+  int fast = -1;  // index of the degree-specialised FP32 variant in use, -1 = generic kernel
+  int generic_only = 0;
   int grid = 0;
   size_t smem = 0;
   void* trace[2] = {nullptr, nullptr};
@@ -433,8 +439,45 @@ int launch_stage_t(bb_solver* s, int mode, int stage, double dt, void* q, void* 
   return bb_check_launch(ctx, "stage_kernel");
 }
 
+int launch_fast(bb_solver* s, int mode, int stage, double dt, void* q, void* res, void* rhs,
+                const void* tin, void* tout, cudaStream_t st) {
+  FastStageParams P;
+  const DegTables& t = *s->tab;
+  P.gtab = t.d_words;
+  P.o_node3 = t.o_node3;
+  P.o_node3m1 = t.o_node3m1;
+  P.o_fvol = t.o_fvol;
+  P.o_fperm = t.o_fperm;
+  P.K = s->K;
+  P.mode = mode;
+  P.rkA = float(mode ? kRK4A[stage] : 0.0);
+  P.rkB = float(mode ? kRK4B[stage] : 0.0);
+  P.dt = float(dt);
+  P.tau = float(s->tau);
+  P.q = (float*)q;
+  P.res = (float*)res;
+  P.rhs = (float*)rhs;
+  P.trace_in = (const float*)tin;
+  P.trace_out = (float*)tout;
+  P.geo = (const float*)s->geo;
+  P.conn = s->conn;
+  P.status = s->d_status;
+  FastLaunch fl;
+  fl.num_sms = s->ctx->num_sms;
+  const int rc = bb_fast_launch(s->fast, fl, P, st);
+  if (rc) return bb_fail(s->ctx, rc, "stage_fast_kernel launch: %s", cudaGetErrorString(cudaGetLastError()));
+  s->ctx->launches++;
+  return BB_OK;
+}
+
+bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
+
 int launch_stage(bb_solver* s, int mode, int stage, double dt, void* q, void* res, void* rhs,
                  const void* tin, void* tout, cudaStream_t st) {
+  // the specialised kernels move tiles with 16-byte-aligned bulk copies
+  if (s->fast >= 0 && aligned16(q) && (!res || aligned16(res)) && aligned16(s->geo) &&
+      aligned16(s->conn))
+    return launch_fast(s, mode, stage, dt, q, res, rhs, tin, tout, st);
   if (s->physics == BB_WAVE)
     return s->dtype == BB_F64
                ? launch_stage_t<double, BB_WAVE>(s, mode, stage, dt, q, res, rhs, tin, tout, st)
@@ -559,6 +602,17 @@ extern "C" int bb_solver_create(bb_ctx* ctx, int physics, int N, int64_t K, int 
     s->epb = 1;
     s->smem = sm;
   }
+  if (dtype == BB_F32) {
+    const int idx = bb_fast_find(N, physics, 0, 0, K);
+    int e = 0, th = 0;
+    size_t sm = 0;
+    if (idx >= 0 && bb_fast_variant_info(idx, &e, &th, &sm) == BB_OK && sm <= ctx->smem_optin) {
+      s->fast = idx;
+      s->epb = e;
+      s->threads = th;
+      s->smem = sm;
+    }
+  }
   s->trace_bytes = (size_t)K * 4 * s->nf * t->Nfp * dtype_size(dtype);
   if (cudaMalloc(&s->trace[0], s->trace_bytes) != cudaSuccess ||
       cudaMalloc(&s->trace[1], s->trace_bytes) != cudaSuccess ||
@@ -589,17 +643,47 @@ extern "C" int bb_solver_destroy(bb_solver* s) {
 
 extern "C" int bb_solver_set_tile(bb_solver* s, int epb, int threads) {
   if (!s) return BB_ERR_ARG;
+  // degree-specialised FP32 variants first, unless the generic kernel was requested
+  if (s->dtype == BB_F32 && !s->generic_only) {
+    const int idx = bb_fast_find(s->N, s->physics, epb, threads, s->K);
+    int e = 0, th = 0;
+    size_t sm = 0;
+    if (idx >= 0 && bb_fast_variant_info(idx, &e, &th, &sm) == BB_OK && sm <= s->ctx->smem_optin) {
+      if (idx != s->fast || e != s->epb) drop_graphs(s);
+      s->fast = idx;
+      s->epb = e;
+      s->threads = th;
+      s->smem = sm;
+      return BB_OK;
+    }
+  }
   if (threads != 0 && threads != kThreads)
-    return bb_fail(s->ctx, BB_ERR_ARG, "threads per block must be %d", kThreads);
+    return bb_fail(s->ctx, BB_ERR_ARG, "no variant with %d threads per block", threads);
   if (epb == 0) epb = 6;
   if (epb < 1 || epb > 64) return bb_fail(s->ctx, BB_ERR_ARG, "elements per block must be 1..64");
   size_t sm = 0;
   if (solver_layout(s, epb, &sm) != BB_OK)
     return bb_fail(s->ctx, BB_ERR_ARG, "tile of %d elements exceeds shared memory", epb);
-  if (epb != s->epb) drop_graphs(s);
+  if (epb != s->epb || s->fast >= 0) drop_graphs(s);
+  s->fast = -1;
   s->epb = epb;
+  s->threads = kThreads;
   s->smem = sm;
   return BB_OK;
+}
+
+extern "C" int bb_solver_set_kernel(bb_solver* s, int kind) {
+  if (!s) return BB_ERR_ARG;
+  if (kind != 0 && kind != 1) return bb_fail(s->ctx, BB_ERR_ARG, "kind must be 0 or 1");
+  s->generic_only = kind;
+  if (kind == 1 && s->fast >= 0) return bb_solver_set_tile(s, s->epb, kThreads);
+  if (kind == 0 && s->fast < 0 && s->dtype == BB_F32 && bb_fast_find(s->N, s->physics, 0, 0, s->K) >= 0)
+    return bb_solver_set_tile(s, 0, 0);
+  return BB_OK;
+}
+
+extern "C" int bb_solver_get_kernel(const bb_solver* s) {
+  return s ? (s->fast >= 0 ? 0 : 1) : -1;
 }
 
 extern "C" int bb_solver_get_tile(const bb_solver* s, int* epb, int* threads) {
@@ -615,7 +699,13 @@ extern "C" int bb_rhs(bb_solver* s, const void* q, void* rhs, void* stream) {
   int rc = bb_set_device(s->ctx);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
-  rc = launch_stage(s, 0, 0, 0.0, const_cast<void*>(q), nullptr, rhs, nullptr, nullptr, st);
+  const void* tin = nullptr;
+  if (s->fast >= 0) {  // the specialised kernel reads outside-tile traces from the buffer
+    rc = launch_extract(s, q, s->trace[0], st);
+    if (rc) return rc;
+    tin = s->trace[0];
+  }
+  rc = launch_stage(s, 0, 0, 0.0, const_cast<void*>(q), nullptr, rhs, tin, nullptr, st);
   if (rc) return rc;
   return check_status(s, st);
 }

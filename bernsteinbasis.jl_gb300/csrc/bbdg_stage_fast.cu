@@ -1,0 +1,601 @@
+// Degree-specialised FP32 stage kernel: fused DG right-hand side + LSRK stage.
+//
+// Same algorithm and data layout as the generic stage kernel (bbdg_solver.cu) with the
+// degree N a compile-time constant, which turns every multi-index computation into an
+// immediate and lets one thread run a whole face lift chain in registers:
+//
+//   lift, per face f and chain c (src/BernsteinLift.jl:139-164):
+//     E0 = L0 x,  L0 = (N+1)^2/2 R_{N+1} E_{N->N+1}, applied as its 7-point stencil
+//         L0 x(i,j) = 1/2 [((i+1)^2+(j+1)^2+(k+1)^2) x(i,j) + (i+1) j x(i+1,j-1)
+//                          + (i+1) k x(i+1,j) + (j+1) i x(i-1,j+1) + (j+1) k x(i,j+1)
+//                          + (k+1) i x(i-1,j) + (k+1) j x(i,j-1)],   k = N-i-j
+//     E_d = R_{N-d+1} E_{d-1} in registers; layer d of the face's volume stack = l_d E_d
+//   the four face stacks are then summed through the permutations of
+//   src/BernsteinLift.jl:207-218 by one thread per volume coefficient, together with the
+//   volume term and the LSRK update.
+//
+// Wave (examples/3d_wave.jl:45-54): with affine elements the scaled normal n is constant on
+// a face, so the u, v, w fluxes are B n_x, B n_y, B n_z with B = (cu n.du - dp)/2: two chains
+// per face (A = (cp dp - n.du)/2 and B) instead of four.
+// Maxwell (examples/3d_maxwell.jl:189-207): six flux components, six chains per face.
+#include <cmath>
+
+#include "bbdg_internal.cuh"
+#include "bbdg_stage_fast.cuh"
+
+namespace {
+
+__host__ __device__ constexpr int c_tri(int n, int j) { return j * (2 * n + 3 - j) / 2; }
+__host__ __device__ constexpr int c_tet(int n, int k) {
+  return ((n + 1) * (n + 2) * (n + 3) - (n + 1 - k) * (n + 2 - k) * (n + 3 - k)) / 6;
+}
+__host__ __device__ constexpr int c_ij(int n, int i, int j) { return i + c_tri(n, j); }
+__host__ __device__ constexpr int c_ijk(int n, int i, int j, int k) { return i + c_tri(n, j) + c_tet(n, k) - j * k; }
+__host__ __device__ constexpr double c_binom(int n, int k) {
+  double b = 1.0;
+  for (int m = 1; m <= k; ++m) b = b * (n - k + m) / m;
+  return b;
+}
+// l_j(N) of src/constants.jl:10-12
+__host__ __device__ constexpr float c_lj(int N, int d) {
+  return float(((d % 2) ? -1.0 : 1.0) * c_binom(N, d) / (1.0 + d));
+}
+
+template <int PHYS>
+struct FPhys;
+template <>
+struct FPhys<BB_WAVE> {
+  static constexpr int NF = 4, NCH = 2, NW = 4;
+};
+template <>
+struct FPhys<BB_MAXWELL> {
+  static constexpr int NF = 6, NCH = 6, NW = 6;
+};
+
+template <int N, int PHYS, int EPB>
+struct FastLayout {
+  static constexpr int NP = (N + 1) * (N + 2) * (N + 3) / 6;
+  static constexpr int NFP = (N + 1) * (N + 2) / 2;
+  static constexpr int NPM1 = N * (N + 1) * (N + 2) / 6;
+  static constexpr int NF = FPhys<PHYS>::NF, NCH = FPhys<PHYS>::NCH, NW = FPhys<PHYS>::NW;
+  static constexpr int NCHAIN = EPB * 4 * NCH;
+  static constexpr int NPS = NP | 1;  // chain stack stride: odd, so same-offset accesses of
+                                      // 32 chain threads fall in 32 different banks
+  // bytes; every TMA destination starts on a 16-byte boundary
+  static constexpr int QBYTES = NF * EPB * NP * 4;            // q tile, [NF][EPB][NP]
+  static constexpr int GEOBYTES = EPB * BB_GEO_STRIDE * 4;     // [EPB][24]
+  static constexpr int CONNBYTES = EPB * 16;                   // [EPB][4] int32
+  static constexpr int SLOT = ((QBYTES + GEOBYTES + CONNBYTES) + 15) / 16 * 16;
+  static constexpr int RES_B = 2 * SLOT;                       // after the two prefetch slots:
+                                                               // res tile [NF][EPB][NP]
+  static constexpr int G_B = RES_B + QBYTES;                   // chain stacks [NCHAIN][NPS]
+  static constexpr int NPM1P = NPM1 + 1;  // volume rows end with a zero entry (index NPM1)
+  static constexpr int W_B = G_B + (NCHAIN * NPS * 4 + 15) / 16 * 16;  // [NW][EPB][NPM1P]
+  static constexpr int GA_B = W_B + (NW * EPB * NPM1P * 4 + 15) / 16 * 16;  // [NP] uint4
+  static constexpr int GW_B = GA_B + NP * 16;                  // [NP] float4 weights
+  static constexpr int VN_B = GW_B + NP * 16;                  // [NPM1] uint2
+  static constexpr int FVOL_B = VN_B + NPM1 * 8;               // [4][NFP] u16
+  static constexpr int FPERM_B = FVOL_B + ((4 * NFP * 2 + 3) / 4 * 4);  // [6][NFP] u16
+  static constexpr int BAR_B = (FPERM_B + 6 * NFP * 2 + 15) / 16 * 16;  // 3 mbarriers
+  static constexpr int BYTES = BAR_B + 32;
+  static_assert((EPB * NP * 4) % 16 == 0, "tile segments must be multiples of 16 bytes");
+};
+
+// ---- TMA bulk copies and mbarriers (inline PTX) ------------------------------------
+__device__ __forceinline__ uint32_t s_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(s_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(s_addr(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(s_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for the phase with the given parity: about a second at most, then false.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (uint32_t it = 0; it < (1u << 24); ++it) {
+    if (mbar_test(bar, parity)) return true;
+    if (it > 64) __nanosleep(64);
+  }
+  return false;
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tma_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          s_addr(dst)),
+      "l"(src), "r"(bytes), "r"(s_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_store(void* dst, const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst),
+               "r"(s_addr(src)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void tma_store_commit() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void tma_store_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+__device__ __forceinline__ void tma_store_wait_all() {
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
+// One face lift chain for compile-time N: reads the chain input x (NFP values, smem), and
+// writes the face's volume stack g[c_ijk(N,i,j,d)] = l_d E_d(i,j) (NP values, smem).
+// x may alias the tail of g: all of x is read before g is written.
+template <int N>
+__device__ __forceinline__ void lift_chain(const float* x, float* g) {
+  constexpr int NFP = (N + 1) * (N + 2) / 2;
+  float X[NFP];
+#pragma unroll
+  for (int m = 0; m < NFP; ++m) X[m] = x[m];
+  float E[NFP];
+#pragma unroll
+  for (int j = 0; j <= N; ++j) {
+#pragma unroll
+    for (int i = 0; i + j <= N; ++i) {
+      const int k = N - i - j;
+      float v = float((i + 1) * (i + 1) + (j + 1) * (j + 1) + (k + 1) * (k + 1)) * X[c_ij(N, i, j)];
+      if (j > 0) v = fmaf(float((i + 1) * j), X[c_ij(N, i + 1, j - 1)], v);
+      if (k > 0) v = fmaf(float((i + 1) * k), X[c_ij(N, i + 1, j)], v);
+      if (i > 0) v = fmaf(float((j + 1) * i), X[c_ij(N, i - 1, j + 1)], v);
+      if (k > 0) v = fmaf(float((j + 1) * k), X[c_ij(N, i, j + 1)], v);
+      if (i > 0) v = fmaf(float((k + 1) * i), X[c_ij(N, i - 1, j)], v);
+      if (j > 0) v = fmaf(float((k + 1) * j), X[c_ij(N, i, j - 1)], v);
+      E[c_ij(N, i, j)] = 0.5f * v;
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < NFP; ++m) g[m] = E[m];  // layer 0 (c_ijk(N,i,j,0) = c_ij(N,i,j))
+#pragma unroll
+  for (int d = 1; d <= N; ++d) {
+    const int n = N - d + 1;  // input degree; E indexed with the degree-N layout
+    const float inv = 1.0f / float(n);
+    const float lj = c_lj(N, d);
+#pragma unroll
+    for (int j = 0; j < n; ++j) {
+#pragma unroll
+      for (int i = 0; i + j < n; ++i) {
+        // reduction_multiply! (src/BernsteinLift.jl:81-85), in place in ascending order
+        const float v = float(i + 1) * inv * E[c_ij(N, i + 1, j)] +
+                        (float(j + 1) * inv * E[c_ij(N, i, j + 1)] +
+                         float(n - i - j) * inv * E[c_ij(N, i, j)]);
+        E[c_ij(N, i, j)] = v;
+        g[c_ijk(N, i, j, d)] = lj * v;
+      }
+    }
+  }
+}
+
+template <int N, int PHYS, int EPB, int NT>
+__global__ void __launch_bounds__(NT) stage_fast_kernel(FastStageParams P) {
+  using L = FastLayout<N, PHYS, EPB>;
+  constexpr int NP = L::NP, NFP = L::NFP, NPM1 = L::NPM1, NF = L::NF, NCH = L::NCH;
+  constexpr int NPS = L::NPS, NCHAIN = L::NCHAIN, NW = L::NW;
+  static_assert(NCHAIN < NT, "need threads beyond the chain threads");
+  constexpr int NITEM = EPB * 4 * NFP;              // face nodes of a tile
+  constexpr int IPT = (NITEM + NT - 1) / NT;        // face nodes per thread
+  extern __shared__ __align__(16) unsigned char smem[];
+  float* sRes = reinterpret_cast<float*>(smem + L::RES_B);
+  float* sG = reinterpret_cast<float*>(smem + L::G_B);
+  float* sW = reinterpret_cast<float*>(smem + L::W_B);
+  // per coefficient alpha: degree N-1 indices of alpha - e_b (NPM1 = zero entry when
+  // alpha_b = 0) and the face-stack positions; weights alpha_b as floats; per beta of
+  // degree N-1: degree N indices of beta + e_a
+  uint4* sGA = reinterpret_cast<uint4*>(smem + L::GA_B);
+  float4* sGW = reinterpret_cast<float4*>(smem + L::GW_B);
+  uint2* sVN = reinterpret_cast<uint2*>(smem + L::VN_B);
+  uint16_t* sFvol = reinterpret_cast<uint16_t*>(smem + L::FVOL_B);
+  uint16_t* sFperm = reinterpret_cast<uint16_t*>(smem + L::FPERM_B);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L::BAR_B);  // [0],[1] slots, [2] res
+  const int tid = threadIdx.x;
+  const int64_t K = P.K;
+  const int64_t ntiles = K / EPB;  // the host guarantees K % EPB == 0
+  const bool stage = P.mode != 0;
+
+  auto slot_q = [](int s) { return reinterpret_cast<float*>(smem + s * L::SLOT); };
+  auto slot_geo = [](int s) {
+    return reinterpret_cast<float*>(smem + s * L::SLOT + L::QBYTES);
+  };
+  auto slot_conn = [](int s) {
+    return reinterpret_cast<int32_t*>(smem + s * L::SLOT + L::QBYTES + L::GEOBYTES);
+  };
+  const float* gq = P.q;
+  const float* gres = P.res;
+  const float* ggeo = P.geo;
+  const int32_t* gconn = P.conn;
+  // tile t's q, geometry and connectivity -> slot s (thread 0 only)
+  auto issue_main = [=](int64_t t, int s) {
+    const int64_t e0 = t * EPB;
+    mbar_expect_tx(&bar[s], L::QBYTES + L::GEOBYTES + L::CONNBYTES);
+#pragma unroll
+    for (int m = 0; m < NF; ++m)
+      tma_load(slot_q(s) + m * EPB * NP, gq + ((size_t)m * K + e0) * NP, EPB * NP * 4, &bar[s]);
+    tma_load(slot_geo(s), ggeo + e0 * BB_GEO_STRIDE, L::GEOBYTES, &bar[s]);
+    tma_load(slot_conn(s), gconn + e0 * 4, L::CONNBYTES, &bar[s]);
+  };
+  auto issue_res = [=](int64_t t) {
+    const int64_t e0 = t * EPB;
+    mbar_expect_tx(&bar[2], L::QBYTES);
+#pragma unroll
+    for (int m = 0; m < NF; ++m)
+      tma_load(sRes + m * EPB * NP, gres + ((size_t)m * K + e0) * NP, EPB * NP * 4, &bar[2]);
+  };
+
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init(&bar[2], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    fence_async_smem();
+  }
+  // constant tables (built from the degree tables in global memory)
+  {
+    const uint32_t* gw = P.gtab;
+    constexpr uint32_t Z = NPM1;
+    for (int t = tid; t < NP; t += NT) {
+      const uint32_t c = gw[P.o_node3 + t];
+      const int i = c & 0xff, j = (c >> 8) & 0xff, k = c >> 16, l = N - i - j - k;
+      const uint32_t m0 = i > 0 ? ijk3(N - 1, i - 1, j, k) : Z;
+      const uint32_t m1 = j > 0 ? ijk3(N - 1, i, j - 1, k) : Z;
+      const uint32_t m2 = k > 0 ? ijk3(N - 1, i, j, k - 1) : Z;
+      const uint32_t m3 = l > 0 ? ijk3(N - 1, i, j, k) : Z;
+      // stack positions of this coefficient on faces f0 (i,k,j), f1 (j,k,l), f2 (j,k,i)
+      const uint32_t p0 = ijk3(N, i, k, j), p1 = ijk3(N, j, k, l), p2 = ijk3(N, j, k, i);
+      sGA[t] = make_uint4(m0 | (m1 << 16), m2 | (m3 << 16), 0u, p0 | (p1 << 10) | (p2 << 20));
+      sGW[t] = make_float4(float(i), float(j), float(k), float(l));
+    }
+    for (int t = tid; t < NPM1; t += NT) {
+      const uint32_t c = gw[P.o_node3m1 + t];
+      const int i = c & 0xff, j = (c >> 8) & 0xff, k = c >> 16;
+      sVN[t] = make_uint2(ijk3(N, i + 1, j, k) | (ijk3(N, i, j + 1, k) << 16),
+                          ijk3(N, i, j, k + 1) | (ijk3(N, i, j, k) << 16));
+    }
+    for (int t = tid; t < NW * EPB; t += NT) sW[t * L::NPM1P + NPM1] = 0.f;
+    const uint16_t* gf = reinterpret_cast<const uint16_t*>(gw + P.o_fvol);
+    for (int t = tid; t < 4 * NFP; t += NT) sFvol[t] = gf[t];
+    const uint16_t* gp = reinterpret_cast<const uint16_t*>(gw + P.o_fperm);
+    for (int t = tid; t < 6 * NFP; t += NT) sFperm[t] = gp[t];
+  }
+  __syncthreads();
+  if (tid == 0 && (int64_t)blockIdx.x < ntiles) {
+    issue_main(blockIdx.x, 0);
+    if (stage) issue_res(blockIdx.x);
+  }
+  uint32_t ph = 0u;  // bit b: parity of the phase barrier b waits for next
+  bool failed = false;
+  const float rkA = P.rkA, rkB = P.rkB, dt = P.dt, tau = P.tau;
+
+  int it = 0;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+    const int s = it & 1;
+    const int64_t e0 = tile * EPB;
+    const int64_t tnext = tile + gridDim.x;
+    float* sQ = slot_q(s);
+    const float* sGeo = slot_geo(s);
+    const int32_t* sConn = slot_conn(s);
+    // ---- 1. wait for this tile, prefetch the next one into the other slot ------------
+    failed = __syncthreads_or(!mbar_wait(&bar[s], (ph >> s) & 1u));
+    if (failed) break;
+    ph ^= 1u << s;
+    if (tid == 0 && tnext < ntiles) {
+      tma_store_wait_read();  // bulk stores of the other slot have read it
+      fence_async_smem();
+      issue_main(tnext, s ^ 1);
+    }
+
+    // ---- 2. interface flux -> chain inputs (tail of each chain's stack) ---------------
+    // outside-tile neighbour traces: all global loads of a thread issued before use
+    float tr[IPT][NF];
+#pragma unroll
+    for (int r = 0; r < IPT; ++r) {
+      const int item = tid + r * NT;
+      if (item < NITEM) {
+        const int le = item / (4 * NFP);
+        const int rem = item - le * 4 * NFP;
+        const int f = rem / NFP, a = rem - f * NFP;
+        const int32_t c = sConn[le * 4 + f];
+        const int64_t nbr = (int64_t)((uint32_t)c >> 5);
+        const int nface = (c >> 3) & 3, o = c & 7;
+        if ((nbr < e0 || nbr >= e0 + EPB) && nbr < K && o <= 5) {
+          const float* tp =
+              P.trace_in + ((size_t)nbr * 4 + nface) * NF * NFP + sFperm[o * NFP + a];
+#pragma unroll
+          for (int m = 0; m < NF; ++m) tr[r][m] = __ldg(tp + m * NFP);
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < IPT; ++r) {
+      const int item = tid + r * NT;
+      if (item >= NITEM) continue;
+      const int le = item / (4 * NFP);
+      const int rem = item - le * 4 * NFP;
+      const int f = rem / NFP, a = rem - f * NFP;
+      const int32_t c = sConn[le * 4 + f];
+      const int64_t nbr = (int64_t)((uint32_t)c >> 5);
+      const int nface = (c >> 3) & 3, o = c & 7;
+      float d[NF];
+      const float* qM = sQ + le * NP + sFvol[f * NFP + a];
+      if (nbr >= K || o > 5) {
+        atomicOr(P.status, 1);
+#pragma unroll
+        for (int m = 0; m < NF; ++m) d[m] = 0.f;
+      } else if (nbr >= e0 && nbr < e0 + EPB) {
+        const float* qP = sQ + (int)(nbr - e0) * NP + sFvol[nface * NFP + sFperm[o * NFP + a]];
+#pragma unroll
+        for (int m = 0; m < NF; ++m) d[m] = qP[m * EPB * NP] - qM[m * EPB * NP];
+      } else {
+#pragma unroll
+        for (int m = 0; m < NF; ++m) d[m] = tr[r][m] - qM[m * EPB * NP];
+      }
+      const float* g = sGeo + le * BB_GEO_STRIDE;
+      const float nx = g[12 + f], ny = g[16 + f], nz = g[20 + f];
+      float cp = 1.f, cu = 1.f;
+      if (tau > 0.f) {
+        const float Jf = sqrtf(nx * nx + ny * ny + nz * nz);
+        cp = tau * Jf;
+        cu = tau / Jf;
+      }
+      float* xin = sG + ((le * 4 + f) * NCH) * NPS + (NPS - NFP) + a;
+      if constexpr (PHYS == BB_WAVE) {
+        const float ndotdU = nx * d[1] + ny * d[2] + nz * d[3];
+        xin[0] = 0.5f * (cp * d[0] - ndotdU);    // p flux
+        xin[NPS] = 0.5f * (cu * ndotdU - d[0]);  // (u,v,w) flux / n
+      } else {
+        const float Hx = d[0], Hy = d[1], Hz = d[2], Ex = d[3], Ey = d[4], Ez = d[5];
+        const float ndH = nx * Hx + ny * Hy + nz * Hz;
+        const float ndE = nx * Ex + ny * Ey + nz * Ez;
+        const float ax[6] = {0.f, Ez, -Ey, 0.f, -Hz, Hy};
+        const float ay[6] = {-Ez, 0.f, Ex, Hz, 0.f, -Hx};
+        const float az[6] = {Ey, -Ex, 0.f, -Hy, Hx, 0.f};
+        const float nd[6] = {ndH * nx, ndH * ny, ndH * nz, ndE * nx, ndE * ny, ndE * nz};
+#pragma unroll
+        for (int m = 0; m < 6; ++m)
+          xin[m * NPS] = 0.5f * ax[m] * nx + 0.5f * ay[m] * ny + 0.5f * az[m] * nz +
+                         0.5f * (cp * d[m]) - 0.5f * (cu * nd[m]);
+      }
+    }
+    __syncthreads();
+
+    // ---- 3. lift chains (threads < NCHAIN) || volume term at degree N-1 (the rest) ----
+    if (tid < NCHAIN) {
+      lift_chain<N>(sG + tid * NPS + (NPS - NFP), sG + tid * NPS);
+    } else {
+      for (int item = tid - NCHAIN; item < EPB * NPM1; item += NT - NCHAIN) {
+        const int le = item / NPM1, b = item - le * NPM1;
+        const uint2 vn = sVN[b];
+        const int idx[4] = {(int)(vn.x & 0xffff), (int)(vn.x >> 16), (int)(vn.y & 0xffff),
+                            (int)(vn.y >> 16)};
+        const float* g = sGeo + le * BB_GEO_STRIDE;
+        // barycentric weights of J d/dx, J d/dy, J d/dz: g_a = (rxJ, sxJ, txJ, -sum)/2; the
+        // sum over a is formed as sum_{a<3} g_a (x_a - x_3), which cancels smooth data
+        const float gx[3] = {0.5f * g[0], 0.5f * g[1], 0.5f * g[2]};
+        const float gy[3] = {0.5f * g[3], 0.5f * g[4], 0.5f * g[5]};
+        const float gz[3] = {0.5f * g[6], 0.5f * g[7], 0.5f * g[8]};
+        const float* q0 = sQ + le * NP;
+        float w[NW];
+#pragma unroll
+        for (int m = 0; m < NW; ++m) w[m] = 0.f;
+        if constexpr (PHYS == BB_WAVE) {
+          const float p3 = q0[idx[3]], u3 = q0[EPB * NP + idx[3]], v3 = q0[2 * EPB * NP + idx[3]],
+                      w3 = q0[3 * EPB * NP + idx[3]];
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            const float p = q0[idx[a]] - p3, u = q0[EPB * NP + idx[a]] - u3,
+                        v = q0[2 * EPB * NP + idx[a]] - v3, ww = q0[3 * EPB * NP + idx[a]] - w3;
+            w[0] += gx[a] * u + gy[a] * v + gz[a] * ww;
+            w[1] += gx[a] * p;
+            w[2] += gy[a] * p;
+            w[3] += gz[a] * p;
+          }
+        } else {
+          float x3[6];
+#pragma unroll
+          for (int m = 0; m < 6; ++m) x3[m] = q0[m * EPB * NP + idx[3]];
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            const float Hx = q0[idx[a]] - x3[0], Hy = q0[EPB * NP + idx[a]] - x3[1],
+                        Hz = q0[2 * EPB * NP + idx[a]] - x3[2];
+            const float Ex = q0[3 * EPB * NP + idx[a]] - x3[3],
+                        Ey = q0[4 * EPB * NP + idx[a]] - x3[4],
+                        Ez = q0[5 * EPB * NP + idx[a]] - x3[5];
+            w[0] += -gy[a] * Ez + gz[a] * Ey;
+            w[1] += gx[a] * Ez - gz[a] * Ex;
+            w[2] += -gx[a] * Ey + gy[a] * Ex;
+            w[3] += gy[a] * Hz - gz[a] * Hy;
+            w[4] += -gx[a] * Hz + gz[a] * Hx;
+            w[5] += gx[a] * Hy - gy[a] * Hx;
+          }
+        }
+#pragma unroll
+        for (int m = 0; m < NW; ++m) sW[(m * EPB + le) * L::NPM1P + b] = w[m];
+      }
+    }
+    __syncthreads();
+    if (stage) {
+      failed = __syncthreads_or(!mbar_wait(&bar[2], (ph >> 2) & 1u));
+      if (failed) break;
+      ph ^= 4u;
+    }
+
+    // ---- 4. gather lift + volume, divide by J, LSRK update ---------------------------
+    for (int item = tid; item < EPB * NP; item += NT) {
+      const int le = item / NP, n = item - le * NP;
+      const uint4 ga = sGA[n];
+      const float4 gw4 = sGW[n];
+      const int x0 = ga.x & 0xffff, x1 = ga.x >> 16, x2 = ga.y & 0xffff, x3 = ga.y >> 16;
+      const float* wb = sW + le * L::NPM1P;
+      float acc[NW];
+#pragma unroll
+      for (int m = 0; m < NW; ++m) {
+        const float* wm = wb + m * EPB * L::NPM1P;
+        acc[m] = fmaf(gw4.x, wm[x0], fmaf(gw4.y, wm[x1], fmaf(gw4.z, wm[x2], gw4.w * wm[x3])));
+      }
+      const uint32_t pos = ga.w;
+      const int p[4] = {(int)(pos & 1023), (int)((pos >> 10) & 1023), (int)(pos >> 20), n};
+      const float* G = sG + le * 4 * NCH * NPS;
+      const float* g = sGeo + le * BB_GEO_STRIDE;
+      const float invJ = g[9];
+      float rhs[NF];
+      if constexpr (PHYS == BB_WAVE) {
+        // face order of src/BernsteinLift.jl:202-214: t=-1 face first, then f1, f2, f3
+        const float B3 = G[(3 * 2 + 1) * NPS + p[3]];
+        float A = G[(3 * 2 + 0) * NPS + p[3]];
+        float Bx = g[12 + 3] * B3, By = g[16 + 3] * B3, Bz = g[20 + 3] * B3;
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+          const float Bf = G[(f * 2 + 1) * NPS + p[f]];
+          A += G[(f * 2 + 0) * NPS + p[f]];
+          Bx = fmaf(g[12 + f], Bf, Bx);
+          By = fmaf(g[16 + f], Bf, By);
+          Bz = fmaf(g[20 + f], Bf, Bz);
+        }
+        rhs[0] = (A - acc[0]) * invJ;
+        rhs[1] = (Bx - acc[1]) * invJ;
+        rhs[2] = (By - acc[2]) * invJ;
+        rhs[3] = (Bz - acc[3]) * invJ;
+      } else {
+#pragma unroll
+        for (int m = 0; m < 6; ++m) {
+          float v = G[(3 * 6 + m) * NPS + p[3]];
+#pragma unroll
+          for (int f = 0; f < 3; ++f) v += G[(f * 6 + m) * NPS + p[f]];
+          rhs[m] = (v + acc[m]) * invJ;
+        }
+      }
+      if (!stage) {
+#pragma unroll
+        for (int m = 0; m < NF; ++m) P.rhs[((size_t)m * K + e0) * NP + item] = rhs[m];
+      } else {
+#pragma unroll
+        for (int m = 0; m < NF; ++m) {
+          const float r = fmaf(rkA, sRes[m * EPB * NP + item], dt * rhs[m]);
+          sRes[m * EPB * NP + item] = r;
+          sQ[m * EPB * NP + item] = fmaf(rkB, r, sQ[m * EPB * NP + item]);
+        }
+      }
+    }
+    __syncthreads();
+
+    // ---- 5. write back q and res (bulk stores), then the outgoing traces -------------
+    if (stage) {
+      if (tid == 0) {
+        fence_async_smem();  // make the generic-proxy smem writes visible to the bulk copies
+#pragma unroll
+        for (int m = 0; m < NF; ++m) {
+          tma_store(P.q + ((size_t)m * K + e0) * NP, sQ + m * EPB * NP, EPB * NP * 4);
+          tma_store(P.res + ((size_t)m * K + e0) * NP, sRes + m * EPB * NP, EPB * NP * 4);
+        }
+        tma_store_commit();
+        if (tnext < ntiles) {
+          tma_store_wait_read();  // sRes has been read out; refill it for the next tile
+          fence_async_smem();
+          issue_res(tnext);
+        }
+      }
+      if (P.trace_out) {
+        for (int item = tid; item < EPB * 4 * NFP; item += NT) {
+          const int le = item / (4 * NFP);
+          const int rem = item - le * 4 * NFP;
+          const int f = rem / NFP, a = rem - f * NFP;
+          const int64_t nbr = (int64_t)((uint32_t)sConn[le * 4 + f] >> 5);
+          if (nbr >= e0 && nbr < e0 + EPB) continue;
+          float* dst = P.trace_out + ((size_t)(e0 + le) * 4 + f) * NF * NFP + a;
+          const float* src = sQ + le * NP + sFvol[f * NFP + a];
+#pragma unroll
+          for (int m = 0; m < NF; ++m) dst[m * NFP] = src[m * EPB * NP];
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (failed && tid == 0) {
+    atomicOr(P.status, 2);
+    // let copies still in flight land before the block exits (bounded)
+    for (int b = 0; b < 3; ++b) mbar_wait(&bar[b], (ph >> b) & 1u);
+  }
+  if (tid == 0) tma_store_wait_all();
+}
+
+template <int N, int PHYS, int EPB, int NT>
+int launch_fast_t(const FastLaunch& fl, const FastStageParams& P, cudaStream_t st) {
+  using L = FastLayout<N, PHYS, EPB>;
+  auto kern = stage_fast_kernel<N, PHYS, EPB, NT>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES) !=
+      cudaSuccess)
+    return BB_ERR_CUDA;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, L::BYTES) != cudaSuccess ||
+      per_sm < 1)
+    return BB_ERR_CUDA;
+  if (P.K % EPB != 0) return BB_ERR_ARG;
+  const int64_t ntiles = P.K / EPB;
+  int64_t grid = (int64_t)per_sm * fl.num_sms;
+  if (grid > ntiles) grid = ntiles;
+  kern<<<(int)grid, NT, L::BYTES, st>>>(P);
+  return cudaGetLastError() == cudaSuccess ? BB_OK : BB_ERR_CUDA;
+}
+
+}  // namespace
+
+// Registry of compiled (N, physics, EPB, threads) variants.
+#define BB_FAST_VARIANTS(X)  \
+  X(9, BB_WAVE, 4, 128)      \
+  X(9, BB_WAVE, 4, 256)      \
+  X(9, BB_WAVE, 2, 64)       \
+  X(9, BB_WAVE, 6, 192)      \
+  X(9, BB_MAXWELL, 2, 128)   \
+  X(9, BB_MAXWELL, 2, 256)
+
+int bb_fast_find(int N, int physics, int epb, int threads, int64_t K) {
+  int idx = 0;
+#define BB_FIND(n_, p_, e_, t_)                                                      \
+  if (N == n_ && physics == p_ && (epb == 0 || epb == e_) &&                         \
+      (threads == 0 || threads == t_) && (K <= 0 || K % e_ == 0))                     \
+    return idx;                                                                      \
+  ++idx;
+  BB_FAST_VARIANTS(BB_FIND)
+#undef BB_FIND
+  return -1;
+}
+
+int bb_fast_variant_info(int idx, int* epb, int* threads, size_t* smem) {
+  int i = 0;
+#define BB_INFO(n_, p_, e_, t_)                              \
+  if (idx == i) {                                            \
+    *epb = e_;                                               \
+    *threads = t_;                                           \
+    *smem = FastLayout<n_, p_, e_>::BYTES;                   \
+    return BB_OK;                                            \
+  }                                                          \
+  ++i;
+  BB_FAST_VARIANTS(BB_INFO)
+#undef BB_INFO
+  return BB_ERR_ARG;
+}
+
+int bb_fast_launch(int idx, const FastLaunch& fl, const FastStageParams& P, cudaStream_t st) {
+  int i = 0;
+#define BB_LAUNCH(n_, p_, e_, t_)                                     \
+  if (idx == i) return launch_fast_t<n_, p_, e_, t_>(fl, P, st);      \
+  ++i;
+  BB_FAST_VARIANTS(BB_LAUNCH)
+#undef BB_LAUNCH
+  return BB_ERR_ARG;
+}

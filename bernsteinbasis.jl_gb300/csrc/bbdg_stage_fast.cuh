@@ -1,0 +1,30 @@
+// Interface of the degree-specialised FP32 stage kernels (bbdg_stage_fast.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+struct FastStageParams {
+  const uint32_t* gtab;  // degree tables (DegTables::d_words) and their word offsets
+  int o_node3, o_node3m1, o_fvol, o_fperm;
+  int64_t K;
+  int mode;              // 0: rhs only, 1: LSRK stage update
+  float rkA, rkB, dt, tau;
+  float* q;              // [NF][K][Np]
+  float* res;            // [NF][K][Np]
+  float* rhs;            // mode 0 output
+  const float* trace_in; // [K][4][NF][Nfp], all faces that cross a tile boundary
+  float* trace_out;      // [K][4][NF][Nfp] or nullptr
+  const float* geo;      // [K][BB_GEO_STRIDE]
+  const int32_t* conn;   // [K][4]
+  int* status;
+};
+
+struct FastLaunch {
+  int num_sms;
+};
+
+// Index of the compiled variant for (N, physics, elements per block, threads), 0 = any,
+// usable for K elements (K must be a multiple of the tile; K <= 0: any); -1 if none.
+int bb_fast_find(int N, int physics, int epb, int threads, int64_t K);
+int bb_fast_variant_info(int idx, int* epb, int* threads, size_t* smem);
+int bb_fast_launch(int idx, const FastLaunch& fl, const FastStageParams& P, cudaStream_t st);

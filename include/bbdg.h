@@ -105,9 +105,15 @@ int bb_fused_apply(bb_ctx* ctx, int N, int64_t K, int dtype, const void* x,
 int bb_solver_create(bb_ctx* ctx, int physics, int N, int64_t K, int dtype,
                      const int32_t* conn, const void* geo, double tau, bb_solver** out);
 int bb_solver_destroy(bb_solver* s);
-/* Elements per thread block and threads per block of the stage kernels (0 = default). */
+/* Elements per thread block and threads per block of the stage kernels (0 = default).
+ * FP32 solvers of some degrees have degree-specialised kernels (whole lift chains in
+ * registers, bulk-copy pipelined tiles); those need K to be a multiple of the tile. */
 int bb_solver_set_tile(bb_solver* s, int elems_per_block, int threads);
 int bb_solver_get_tile(const bb_solver* s, int* elems_per_block, int* threads);
+/* kind 0: use a degree-specialised kernel when one exists (default); 1: generic kernel. */
+int bb_solver_set_kernel(bb_solver* s, int kind);
+/* 0 if a degree-specialised kernel is in use, 1 for the generic kernel. */
+int bb_solver_get_kernel(const bb_solver* s);
 
 /* rhs = RHS(q): one evaluation of rhs_matvec! (examples/3d_wave.jl:36-84,
  * examples/3d_maxwell.jl:36-93). */
