@@ -18,11 +18,10 @@ CACHE = os.path.join(_build.BUILD, "autotune.json")
 
 # Candidates (kernel, elements per block, threads per block).
 CANDIDATES = {
-    ("wave", 9, torch.float32): [("specialised", 4, 128), ("specialised", 4, 256),
-                                 ("specialised", 2, 64), ("specialised", 6, 192),
-                                 ("generic", 4, 256), ("generic", 2, 256)],
-    ("maxwell", 9, torch.float32): [("specialised", 2, 128), ("specialised", 2, 256),
-                                    ("generic", 2, 256), ("generic", 4, 256)],
+    ("wave", 9, torch.float32): [("specialised", 4, 288), ("specialised", 4, 160),
+                                 ("specialised", 2, 160), ("generic", 4, 256)],
+    ("maxwell", 9, torch.float32): [("specialised", 2, 192), ("specialised", 2, 256),
+                                    ("generic", 2, 256)],
 }
 GENERIC = [("generic", e, 256) for e in (1, 2, 4, 6, 12)]
 

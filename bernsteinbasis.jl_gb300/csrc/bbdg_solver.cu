@@ -430,12 +430,12 @@ int launch_stage_t(bb_solver* s, int mode, int stage, double dt, void* q, void* 
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total));
   int per_sm = 0;
   BB_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stage_kernel<T, PHYS>,
-                                                             s->threads, L.total));
+                                                             kThreads, L.total));
   if (per_sm < 1) return bb_fail(ctx, BB_ERR_ARG, "tile does not fit on an SM");
   const int64_t ntiles = (s->K + s->epb - 1) / s->epb;
   int64_t grid = (int64_t)per_sm * ctx->num_sms;
   if (grid > ntiles) grid = ntiles;
-  stage_kernel<T, PHYS><<<(int)grid, s->threads, L.total, st>>>(P, L);
+  stage_kernel<T, PHYS><<<(int)grid, kThreads, L.total, st>>>(P, L);
   return bb_check_launch(ctx, "stage_kernel");
 }
 

@@ -9,8 +9,8 @@
 //         L0 x(i,j) = 1/2 [((i+1)^2+(j+1)^2+(k+1)^2) x(i,j) + (i+1) j x(i+1,j-1)
 //                          + (i+1) k x(i+1,j) + (j+1) i x(i-1,j+1) + (j+1) k x(i,j+1)
 //                          + (k+1) i x(i-1,j) + (k+1) j x(i,j-1)],   k = N-i-j
-//     E_d = R_{N-d+1} E_{d-1} in registers; layer d of the face's volume stack = l_d E_d
-//   the four face stacks are then summed through the permutations of
+//     E_d = R_{N-d+1} E_{d-1}, all in registers; the face's volume stack holds E_d at layer d
+//   the four face stacks are summed, with the l_d weights, through the permutations of
 //   src/BernsteinLift.jl:207-218 by one thread per volume coefficient, together with the
 //   volume term and the LSRK update.
 //
@@ -18,6 +18,12 @@
 // a face, so the u, v, w fluxes are B n_x, B n_y, B n_z with B = (cu n.du - dp)/2: two chains
 // per face (A = (cp dp - n.du)/2 and B) instead of four.
 // Maxwell (examples/3d_maxwell.jl:189-207): six flux components, six chains per face.
+//
+// Block organisation: EPB elements per tile; TPE "element threads" per element plus
+// CHT "chain threads" (whole warps, one lift chain each). Tiles stream through a persistent
+// loop: q, geometry and connectivity of the next tile and res of the current one arrive by
+// bulk copies (cp.async.bulk, mbarrier completion, bounded waits); q and res leave by bulk
+// stores.
 #include <cmath>
 
 #include "bbdg_internal.cuh"
@@ -30,15 +36,14 @@ __host__ __device__ constexpr int c_tet(int n, int k) {
   return ((n + 1) * (n + 2) * (n + 3) - (n + 1 - k) * (n + 2 - k) * (n + 3 - k)) / 6;
 }
 __host__ __device__ constexpr int c_ij(int n, int i, int j) { return i + c_tri(n, j); }
-__host__ __device__ constexpr int c_ijk(int n, int i, int j, int k) { return i + c_tri(n, j) + c_tet(n, k) - j * k; }
-__host__ __device__ constexpr double c_binom(int n, int k) {
-  double b = 1.0;
-  for (int m = 1; m <= k; ++m) b = b * (n - k + m) / m;
-  return b;
+__host__ __device__ constexpr int c_ijk(int n, int i, int j, int k) {
+  return i + c_tri(n, j) + c_tet(n, k) - j * k;
 }
 // l_j(N) of src/constants.jl:10-12
-__host__ __device__ constexpr float c_lj(int N, int d) {
-  return float(((d % 2) ? -1.0 : 1.0) * c_binom(N, d) / (1.0 + d));
+__host__ __device__ inline float lift_lj(int N, int d) {
+  double b = 1.0;
+  for (int m = 1; m <= d; ++m) b = b * (N - d + m) / m;
+  return float(((d % 2) ? -1.0 : 1.0) * b / (1.0 + d));
 }
 
 template <int PHYS>
@@ -52,36 +57,42 @@ struct FPhys<BB_MAXWELL> {
   static constexpr int NF = 6, NCH = 6, NW = 6;
 };
 
-template <int N, int PHYS, int EPB>
+template <int N, int PHYS, int EPB, int TPE>
 struct FastLayout {
   static constexpr int NP = (N + 1) * (N + 2) * (N + 3) / 6;
   static constexpr int NFP = (N + 1) * (N + 2) / 2;
   static constexpr int NPM1 = N * (N + 1) * (N + 2) / 6;
   static constexpr int NF = FPhys<PHYS>::NF, NCH = FPhys<PHYS>::NCH, NW = FPhys<PHYS>::NW;
   static constexpr int NCHAIN = EPB * 4 * NCH;
+  static constexpr int CHT = (NCHAIN + 31) / 32 * 32;  // chain threads, whole warps
+  static constexpr int NTE = EPB * TPE;                // element threads
+  static constexpr int NT = NTE + CHT;
   static constexpr int NPS = NP | 1;  // chain stack stride: odd, so same-offset accesses of
-                                      // 32 chain threads fall in 32 different banks
-  // bytes; every TMA destination starts on a 16-byte boundary
+                                      // the chain threads fall in different banks
+  static constexpr int NPM1P = NPM1 + 1;  // volume rows end with a zero entry (index NPM1)
+  // bytes; every bulk-copy destination starts on a 16-byte boundary
   static constexpr int QBYTES = NF * EPB * NP * 4;            // q tile, [NF][EPB][NP]
   static constexpr int GEOBYTES = EPB * BB_GEO_STRIDE * 4;     // [EPB][24]
   static constexpr int CONNBYTES = EPB * 16;                   // [EPB][4] int32
   static constexpr int SLOT = ((QBYTES + GEOBYTES + CONNBYTES) + 15) / 16 * 16;
-  static constexpr int RES_B = 2 * SLOT;                       // after the two prefetch slots:
-                                                               // res tile [NF][EPB][NP]
-  static constexpr int G_B = RES_B + QBYTES;                   // chain stacks [NCHAIN][NPS]
-  static constexpr int NPM1P = NPM1 + 1;  // volume rows end with a zero entry (index NPM1)
+  static constexpr int RES_B = 2 * SLOT;                       // after the two q slots
+  static constexpr int G_B = RES_B + QBYTES;                   // [NCHAIN][NPS] face stacks
   static constexpr int W_B = G_B + (NCHAIN * NPS * 4 + 15) / 16 * 16;  // [NW][EPB][NPM1P]
-  static constexpr int GA_B = W_B + (NW * EPB * NPM1P * 4 + 15) / 16 * 16;  // [NP] uint4
-  static constexpr int GW_B = GA_B + NP * 16;                  // [NP] float4 weights
-  static constexpr int VN_B = GW_B + NP * 16;                  // [NPM1] uint2
+  static constexpr int VOL_B = W_B + (NW * EPB * NPM1P * 4 + 15) / 16 * 16;  // [NW][EPB][NP]
+  static constexpr int GA_B = VOL_B + NW * EPB * NP * 4;       // [NP] uint4
+  static constexpr int GW_B = GA_B + NP * 16;                  // [NP] float4 alpha_b
+  static constexpr int LW_B = GW_B + NP * 16;                  // [NP] float4 l_d per face
+  static constexpr int VN_B = LW_B + NP * 16;                  // [NPM1] uint2
   static constexpr int FVOL_B = VN_B + NPM1 * 8;               // [4][NFP] u16
   static constexpr int FPERM_B = FVOL_B + ((4 * NFP * 2 + 3) / 4 * 4);  // [6][NFP] u16
-  static constexpr int BAR_B = (FPERM_B + 6 * NFP * 2 + 15) / 16 * 16;  // 3 mbarriers
+  static constexpr int FNB_B = FPERM_B + ((6 * NFP * 2 + 3) / 4 * 4);  // [4][6][NFP] u16
+  static constexpr int BAR_B = (FNB_B + 24 * NFP * 2 + 15) / 16 * 16;  // 3 mbarriers
   static constexpr int BYTES = BAR_B + 32;
   static_assert((EPB * NP * 4) % 16 == 0, "tile segments must be multiples of 16 bytes");
+  static_assert(TPE % 32 == 0 && TPE >= 32, "element threads come in whole warps");
 };
 
-// ---- TMA bulk copies and mbarriers (inline PTX) ------------------------------------
+// ---- bulk copies and mbarriers (inline PTX) -----------------------------------------
 __device__ __forceinline__ uint32_t s_addr(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
@@ -134,10 +145,13 @@ __device__ __forceinline__ void tma_store_wait_read() {
 __device__ __forceinline__ void tma_store_wait_all() {
   asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
+__device__ __forceinline__ void named_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
 
-// One face lift chain for compile-time N: reads the chain input x (NFP values, smem), and
-// writes the face's volume stack g[c_ijk(N,i,j,d)] = l_d E_d(i,j) (NP values, smem).
-// x may alias the tail of g: all of x is read before g is written.
+// One face lift chain for compile-time N: x = chain input (NFP values, smem, may alias the
+// tail of g); g = the face's volume stack, g[c_ijk(N,i,j,d)] = E_d(i,j) (unscaled; the
+// l_d factors are applied when the stacks are summed). All of x is read before g is written.
 template <int N>
 __device__ __forceinline__ void lift_chain(const float* x, float* g) {
   constexpr int NFP = (N + 1) * (N + 2) / 2;
@@ -166,7 +180,6 @@ __device__ __forceinline__ void lift_chain(const float* x, float* g) {
   for (int d = 1; d <= N; ++d) {
     const int n = N - d + 1;  // input degree; E indexed with the degree-N layout
     const float inv = 1.0f / float(n);
-    const float lj = c_lj(N, d);
 #pragma unroll
     for (int j = 0; j < n; ++j) {
 #pragma unroll
@@ -176,42 +189,48 @@ __device__ __forceinline__ void lift_chain(const float* x, float* g) {
                         (float(j + 1) * inv * E[c_ij(N, i, j + 1)] +
                          float(n - i - j) * inv * E[c_ij(N, i, j)]);
         E[c_ij(N, i, j)] = v;
-        g[c_ijk(N, i, j, d)] = lj * v;
+        g[c_ijk(N, i, j, d)] = v;
       }
     }
   }
 }
 
-template <int N, int PHYS, int EPB, int NT>
-__global__ void __launch_bounds__(NT) stage_fast_kernel(FastStageParams P) {
-  using L = FastLayout<N, PHYS, EPB>;
+template <int N, int PHYS, int EPB, int TPE>
+__global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT)
+    stage_fast_kernel(FastStageParams P) {
+  using L = FastLayout<N, PHYS, EPB, TPE>;
   constexpr int NP = L::NP, NFP = L::NFP, NPM1 = L::NPM1, NF = L::NF, NCH = L::NCH;
-  constexpr int NPS = L::NPS, NCHAIN = L::NCHAIN, NW = L::NW;
-  static_assert(NCHAIN < NT, "need threads beyond the chain threads");
-  constexpr int NITEM = EPB * 4 * NFP;              // face nodes of a tile
-  constexpr int IPT = (NITEM + NT - 1) / NT;        // face nodes per thread
+  constexpr int NPS = L::NPS, NCHAIN = L::NCHAIN, NW = L::NW, NTE = L::NTE, NT = L::NT;
+  constexpr int FT = TPE / 4;                     // element threads per face
+  constexpr int FR = (NFP + FT - 1) / FT;         // face nodes per element thread
+  constexpr int VR = (NPM1 + TPE - 1) / TPE;      // degree N-1 points per element thread
+  constexpr int GR = (NP + TPE - 1) / TPE;        // coefficients per element thread
   extern __shared__ __align__(16) unsigned char smem[];
   float* sRes = reinterpret_cast<float*>(smem + L::RES_B);
   float* sG = reinterpret_cast<float*>(smem + L::G_B);
   float* sW = reinterpret_cast<float*>(smem + L::W_B);
+  float* sVol = reinterpret_cast<float*>(smem + L::VOL_B);
   // per coefficient alpha: degree N-1 indices of alpha - e_b (NPM1 = zero entry when
-  // alpha_b = 0) and the face-stack positions; weights alpha_b as floats; per beta of
-  // degree N-1: degree N indices of beta + e_a
+  // alpha_b = 0) and face-stack positions; alpha_b; l_d of its layer on each face
   uint4* sGA = reinterpret_cast<uint4*>(smem + L::GA_B);
   float4* sGW = reinterpret_cast<float4*>(smem + L::GW_B);
-  uint2* sVN = reinterpret_cast<uint2*>(smem + L::VN_B);
+  float4* sLW = reinterpret_cast<float4*>(smem + L::LW_B);
+  uint2* sVN = reinterpret_cast<uint2*>(smem + L::VN_B);  // beta -> indices of beta + e_a
   uint16_t* sFvol = reinterpret_cast<uint16_t*>(smem + L::FVOL_B);
   uint16_t* sFperm = reinterpret_cast<uint16_t*>(smem + L::FPERM_B);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L::BAR_B);  // [0],[1] slots, [2] res
+  // partner face nf, orientation o, node a -> volume index of the partner's node
+  uint16_t* sFnb = reinterpret_cast<uint16_t*>(smem + L::FNB_B);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L::BAR_B);  // [0],[1] q slots, [2] res
   const int tid = threadIdx.x;
   const int64_t K = P.K;
   const int64_t ntiles = K / EPB;  // the host guarantees K % EPB == 0
   const bool stage = P.mode != 0;
+  // element threads: element le, lane u within the element
+  const int le = tid / TPE, u = tid - (tid / TPE) * TPE;
+  const bool is_elem = tid < NTE;
 
   auto slot_q = [](int s) { return reinterpret_cast<float*>(smem + s * L::SLOT); };
-  auto slot_geo = [](int s) {
-    return reinterpret_cast<float*>(smem + s * L::SLOT + L::QBYTES);
-  };
+  auto slot_geo = [](int s) { return reinterpret_cast<float*>(smem + s * L::SLOT + L::QBYTES); };
   auto slot_conn = [](int s) {
     return reinterpret_cast<int32_t*>(smem + s * L::SLOT + L::QBYTES + L::GEOBYTES);
   };
@@ -259,6 +278,10 @@ __global__ void __launch_bounds__(NT) stage_fast_kernel(FastStageParams P) {
       const uint32_t p0 = ijk3(N, i, k, j), p1 = ijk3(N, j, k, l), p2 = ijk3(N, j, k, i);
       sGA[t] = make_uint4(m0 | (m1 << 16), m2 | (m3 << 16), 0u, p0 | (p1 << 10) | (p2 << 20));
       sGW[t] = make_float4(float(i), float(j), float(k), float(l));
+      // l_d of the layer this coefficient sits in on faces f0..f3 (distances j, l, i, k);
+      // layer 0 carries the L0 block itself (weight 1)
+      auto lw = [](int d) { return d == 0 ? 1.0f : lift_lj(N, d); };
+      sLW[t] = make_float4(lw(j), lw(l), lw(i), lw(k));
     }
     for (int t = tid; t < NPM1; t += NT) {
       const uint32_t c = gw[P.o_node3m1 + t];
@@ -271,6 +294,11 @@ __global__ void __launch_bounds__(NT) stage_fast_kernel(FastStageParams P) {
     for (int t = tid; t < 4 * NFP; t += NT) sFvol[t] = gf[t];
     const uint16_t* gp = reinterpret_cast<const uint16_t*>(gw + P.o_fperm);
     for (int t = tid; t < 6 * NFP; t += NT) sFperm[t] = gp[t];
+    for (int t = tid; t < 24 * NFP; t += NT) {
+      const int fo = t / NFP, a = t - fo * NFP;
+      const uint16_t* gfv = reinterpret_cast<const uint16_t*>(gw + P.o_fvol);
+      sFnb[t] = gfv[(fo / 6) * NFP + gp[(fo % 6) * NFP + a]];
+    }
   }
   __syncthreads();
   if (tid == 0 && (int64_t)blockIdx.x < ntiles) {
@@ -280,6 +308,8 @@ __global__ void __launch_bounds__(NT) stage_fast_kernel(FastStageParams P) {
   uint32_t ph = 0u;  // bit b: parity of the phase barrier b waits for next
   bool failed = false;
   const float rkA = P.rkA, rkB = P.rkB, dt = P.dt, tau = P.tau;
+  // face handled by this element thread in the flux and trace phases
+  const int ff = u / FT, fa0 = u - (u / FT) * FT;
 
   int it = 0;
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
@@ -299,96 +329,96 @@ __global__ void __launch_bounds__(NT) stage_fast_kernel(FastStageParams P) {
       issue_main(tnext, s ^ 1);
     }
 
-    // ---- 2. interface flux -> chain inputs (tail of each chain's stack) ---------------
-    // outside-tile neighbour traces: all global loads of a thread issued before use
-    float tr[IPT][NF];
+    // ---- 2. interface flux of face ff of element le -> chain inputs -------------------
+    if (is_elem) {
+      const int32_t c = sConn[le * 4 + ff];
+      const int64_t nbr = (int64_t)((uint32_t)c >> 5);
+      const int nface = (c >> 3) & 3, o = c & 7;
+      const bool bad = nbr >= K || o > 5;
+      const bool inside = nbr >= e0 && nbr < e0 + EPB;
+      if (bad && fa0 == 0) atomicOr(P.status, 1);
+      const float* g = sGeo + le * BB_GEO_STRIDE;
+      const float nx = g[12 + ff], ny = g[16 + ff], nz = g[20 + ff];
+      float cp = 1.f, cu = 1.f;
+      if (tau > 0.f) {
+        const float n2 = nx * nx + ny * ny + nz * nz;
+        const float rJf = rsqrtf(n2);
+        cp = tau * n2 * rJf;  // tau |n|
+        cu = tau * rJf;       // tau / |n|
+      }
+      // outside-tile neighbour traces: issue every global load before using any
+      float tr[FR][NF];
+      const float* tbase = P.trace_in + ((size_t)(bad ? 0 : nbr) * 4 + nface) * NF * NFP;
 #pragma unroll
-    for (int r = 0; r < IPT; ++r) {
-      const int item = tid + r * NT;
-      if (item < NITEM) {
-        const int le = item / (4 * NFP);
-        const int rem = item - le * 4 * NFP;
-        const int f = rem / NFP, a = rem - f * NFP;
-        const int32_t c = sConn[le * 4 + f];
-        const int64_t nbr = (int64_t)((uint32_t)c >> 5);
-        const int nface = (c >> 3) & 3, o = c & 7;
-        if ((nbr < e0 || nbr >= e0 + EPB) && nbr < K && o <= 5) {
-          const float* tp =
-              P.trace_in + ((size_t)nbr * 4 + nface) * NF * NFP + sFperm[o * NFP + a];
+      for (int r = 0; r < FR; ++r) {
+        const int a = fa0 + r * FT;
+        if (a < NFP && !inside && !bad) {
+          const float* tp = tbase + sFperm[o * NFP + a];
 #pragma unroll
           for (int m = 0; m < NF; ++m) tr[r][m] = __ldg(tp + m * NFP);
         }
       }
-    }
+      const int pin = (int)(nbr - e0);
+      float* xin0 = sG + ((le * 4 + ff) * NCH) * NPS + (NPS - NFP);
 #pragma unroll
-    for (int r = 0; r < IPT; ++r) {
-      const int item = tid + r * NT;
-      if (item >= NITEM) continue;
-      const int le = item / (4 * NFP);
-      const int rem = item - le * 4 * NFP;
-      const int f = rem / NFP, a = rem - f * NFP;
-      const int32_t c = sConn[le * 4 + f];
-      const int64_t nbr = (int64_t)((uint32_t)c >> 5);
-      const int nface = (c >> 3) & 3, o = c & 7;
-      float d[NF];
-      const float* qM = sQ + le * NP + sFvol[f * NFP + a];
-      if (nbr >= K || o > 5) {
-        atomicOr(P.status, 1);
+      for (int r = 0; r < FR; ++r) {
+        const int a = fa0 + r * FT;
+        if (a >= NFP) continue;
+        float d[NF];
+        const float* qM = sQ + le * NP + sFvol[ff * NFP + a];
+        if (bad) {
 #pragma unroll
-        for (int m = 0; m < NF; ++m) d[m] = 0.f;
-      } else if (nbr >= e0 && nbr < e0 + EPB) {
-        const float* qP = sQ + (int)(nbr - e0) * NP + sFvol[nface * NFP + sFperm[o * NFP + a]];
+          for (int m = 0; m < NF; ++m) d[m] = 0.f;
+        } else if (inside) {
+          const float* qP = sQ + pin * NP + sFnb[(nface * 6 + o) * NFP + a];
 #pragma unroll
-        for (int m = 0; m < NF; ++m) d[m] = qP[m * EPB * NP] - qM[m * EPB * NP];
-      } else {
+          for (int m = 0; m < NF; ++m) d[m] = qP[m * EPB * NP] - qM[m * EPB * NP];
+        } else {
 #pragma unroll
-        for (int m = 0; m < NF; ++m) d[m] = tr[r][m] - qM[m * EPB * NP];
-      }
-      const float* g = sGeo + le * BB_GEO_STRIDE;
-      const float nx = g[12 + f], ny = g[16 + f], nz = g[20 + f];
-      float cp = 1.f, cu = 1.f;
-      if (tau > 0.f) {
-        const float Jf = sqrtf(nx * nx + ny * ny + nz * nz);
-        cp = tau * Jf;
-        cu = tau / Jf;
-      }
-      float* xin = sG + ((le * 4 + f) * NCH) * NPS + (NPS - NFP) + a;
-      if constexpr (PHYS == BB_WAVE) {
-        const float ndotdU = nx * d[1] + ny * d[2] + nz * d[3];
-        xin[0] = 0.5f * (cp * d[0] - ndotdU);    // p flux
-        xin[NPS] = 0.5f * (cu * ndotdU - d[0]);  // (u,v,w) flux / n
-      } else {
-        const float Hx = d[0], Hy = d[1], Hz = d[2], Ex = d[3], Ey = d[4], Ez = d[5];
-        const float ndH = nx * Hx + ny * Hy + nz * Hz;
-        const float ndE = nx * Ex + ny * Ey + nz * Ez;
-        const float ax[6] = {0.f, Ez, -Ey, 0.f, -Hz, Hy};
-        const float ay[6] = {-Ez, 0.f, Ex, Hz, 0.f, -Hx};
-        const float az[6] = {Ey, -Ex, 0.f, -Hy, Hx, 0.f};
-        const float nd[6] = {ndH * nx, ndH * ny, ndH * nz, ndE * nx, ndE * ny, ndE * nz};
+          for (int m = 0; m < NF; ++m) d[m] = tr[r][m] - qM[m * EPB * NP];
+        }
+        float* xin = xin0 + a;
+        if constexpr (PHYS == BB_WAVE) {
+          const float ndotdU = nx * d[1] + ny * d[2] + nz * d[3];
+          xin[0] = 0.5f * (cp * d[0] - ndotdU);    // p flux
+          xin[NPS] = 0.5f * (cu * ndotdU - d[0]);  // (u,v,w) flux / n
+        } else {
+          const float Hx = d[0], Hy = d[1], Hz = d[2], Ex = d[3], Ey = d[4], Ez = d[5];
+          const float ndH = nx * Hx + ny * Hy + nz * Hz;
+          const float ndE = nx * Ex + ny * Ey + nz * Ez;
+          const float ax[6] = {0.f, Ez, -Ey, 0.f, -Hz, Hy};
+          const float ay[6] = {-Ez, 0.f, Ex, Hz, 0.f, -Hx};
+          const float az[6] = {Ey, -Ex, 0.f, -Hy, Hx, 0.f};
+          const float nd[6] = {ndH * nx, ndH * ny, ndH * nz, ndE * nx, ndE * ny, ndE * nz};
 #pragma unroll
-        for (int m = 0; m < 6; ++m)
-          xin[m * NPS] = 0.5f * ax[m] * nx + 0.5f * ay[m] * ny + 0.5f * az[m] * nz +
-                         0.5f * (cp * d[m]) - 0.5f * (cu * nd[m]);
+          for (int m = 0; m < 6; ++m)
+            xin[m * NPS] = 0.5f * ax[m] * nx + 0.5f * ay[m] * ny + 0.5f * az[m] * nz +
+                           0.5f * (cp * d[m]) - 0.5f * (cu * nd[m]);
+        }
       }
     }
     __syncthreads();
 
-    // ---- 3. lift chains (threads < NCHAIN) || volume term at degree N-1 (the rest) ----
-    if (tid < NCHAIN) {
-      lift_chain<N>(sG + tid * NPS + (NPS - NFP), sG + tid * NPS);
+    // ---- 3. chain warps: lift chains || element threads: volume term -----------------
+    if (!is_elem) {
+      const int c = tid - NTE;
+      if (c < NCHAIN) lift_chain<N>(sG + c * NPS + (NPS - NFP), sG + c * NPS);
     } else {
-      for (int item = tid - NCHAIN; item < EPB * NPM1; item += NT - NCHAIN) {
-        const int le = item / NPM1, b = item - le * NPM1;
+      const float* g = sGeo + le * BB_GEO_STRIDE;
+      // barycentric weights of J d/dx, J d/dy, J d/dz: g_a = (rxJ, sxJ, txJ, -sum)/2; the
+      // sum over a is formed as sum_{a<3} g_a (x_a - x_3), which cancels smooth data
+      const float gx[3] = {0.5f * g[0], 0.5f * g[1], 0.5f * g[2]};
+      const float gy[3] = {0.5f * g[3], 0.5f * g[4], 0.5f * g[5]};
+      const float gz[3] = {0.5f * g[6], 0.5f * g[7], 0.5f * g[8]};
+      const float* q0 = sQ + le * NP;
+      // 3a. w(beta) at degree N-1
+#pragma unroll
+      for (int r = 0; r < VR; ++r) {
+        const int b = u + r * TPE;
+        if (b >= NPM1) continue;
         const uint2 vn = sVN[b];
         const int idx[4] = {(int)(vn.x & 0xffff), (int)(vn.x >> 16), (int)(vn.y & 0xffff),
                             (int)(vn.y >> 16)};
-        const float* g = sGeo + le * BB_GEO_STRIDE;
-        // barycentric weights of J d/dx, J d/dy, J d/dz: g_a = (rxJ, sxJ, txJ, -sum)/2; the
-        // sum over a is formed as sum_{a<3} g_a (x_a - x_3), which cancels smooth data
-        const float gx[3] = {0.5f * g[0], 0.5f * g[1], 0.5f * g[2]};
-        const float gy[3] = {0.5f * g[3], 0.5f * g[4], 0.5f * g[5]};
-        const float gz[3] = {0.5f * g[6], 0.5f * g[7], 0.5f * g[8]};
-        const float* q0 = sQ + le * NP;
         float w[NW];
 #pragma unroll
         for (int m = 0; m < NW; ++m) w[m] = 0.f;
@@ -397,9 +427,9 @@ __global__ void __launch_bounds__(NT) stage_fast_kernel(FastStageParams P) {
                       w3 = q0[3 * EPB * NP + idx[3]];
 #pragma unroll
           for (int a = 0; a < 3; ++a) {
-            const float p = q0[idx[a]] - p3, u = q0[EPB * NP + idx[a]] - u3,
+            const float p = q0[idx[a]] - p3, uu = q0[EPB * NP + idx[a]] - u3,
                         v = q0[2 * EPB * NP + idx[a]] - v3, ww = q0[3 * EPB * NP + idx[a]] - w3;
-            w[0] += gx[a] * u + gy[a] * v + gz[a] * ww;
+            w[0] += gx[a] * uu + gy[a] * v + gz[a] * ww;
             w[1] += gx[a] * p;
             w[2] += gy[a] * p;
             w[3] += gz[a] * p;
@@ -426,6 +456,23 @@ __global__ void __launch_bounds__(NT) stage_fast_kernel(FastStageParams P) {
 #pragma unroll
         for (int m = 0; m < NW; ++m) sW[(m * EPB + le) * L::NPM1P + b] = w[m];
       }
+      named_sync(1, NTE);
+      // 3b. vol(alpha) = sum_b alpha_b w(alpha - e_b), the volume part of J * rhs
+      const float* wb = sW + le * L::NPM1P;
+#pragma unroll
+      for (int r = 0; r < GR; ++r) {
+        const int n = u + r * TPE;
+        if (n >= NP) continue;
+        const uint4 ga = sGA[n];
+        const float4 gw4 = sGW[n];
+        const int x0 = ga.x & 0xffff, x1 = ga.x >> 16, x2 = ga.y & 0xffff, x3 = ga.y >> 16;
+#pragma unroll
+        for (int m = 0; m < NW; ++m) {
+          const float* wm = wb + m * EPB * L::NPM1P;
+          sVol[(m * EPB + le) * NP + n] =
+              fmaf(gw4.x, wm[x0], fmaf(gw4.y, wm[x1], fmaf(gw4.z, wm[x2], gw4.w * wm[x3])));
+        }
+      }
     }
     __syncthreads();
     if (stage) {
@@ -434,60 +481,65 @@ __global__ void __launch_bounds__(NT) stage_fast_kernel(FastStageParams P) {
       ph ^= 4u;
     }
 
-    // ---- 4. gather lift + volume, divide by J, LSRK update ---------------------------
-    for (int item = tid; item < EPB * NP; item += NT) {
-      const int le = item / NP, n = item - le * NP;
-      const uint4 ga = sGA[n];
-      const float4 gw4 = sGW[n];
-      const int x0 = ga.x & 0xffff, x1 = ga.x >> 16, x2 = ga.y & 0xffff, x3 = ga.y >> 16;
-      const float* wb = sW + le * L::NPM1P;
-      float acc[NW];
-#pragma unroll
-      for (int m = 0; m < NW; ++m) {
-        const float* wm = wb + m * EPB * L::NPM1P;
-        acc[m] = fmaf(gw4.x, wm[x0], fmaf(gw4.y, wm[x1], fmaf(gw4.z, wm[x2], gw4.w * wm[x3])));
-      }
-      const uint32_t pos = ga.w;
-      const int p[4] = {(int)(pos & 1023), (int)((pos >> 10) & 1023), (int)(pos >> 20), n};
-      const float* G = sG + le * 4 * NCH * NPS;
+    // ---- 4. sum lift stacks + volume term, divide by J, LSRK update ------------------
+    if (is_elem) {
       const float* g = sGeo + le * BB_GEO_STRIDE;
       const float invJ = g[9];
-      float rhs[NF];
-      if constexpr (PHYS == BB_WAVE) {
-        // face order of src/BernsteinLift.jl:202-214: t=-1 face first, then f1, f2, f3
-        const float B3 = G[(3 * 2 + 1) * NPS + p[3]];
-        float A = G[(3 * 2 + 0) * NPS + p[3]];
-        float Bx = g[12 + 3] * B3, By = g[16 + 3] * B3, Bz = g[20 + 3] * B3;
+      float nxf[4], nyf[4], nzf[4];
 #pragma unroll
-        for (int f = 0; f < 3; ++f) {
-          const float Bf = G[(f * 2 + 1) * NPS + p[f]];
-          A += G[(f * 2 + 0) * NPS + p[f]];
-          Bx = fmaf(g[12 + f], Bf, Bx);
-          By = fmaf(g[16 + f], Bf, By);
-          Bz = fmaf(g[20 + f], Bf, Bz);
-        }
-        rhs[0] = (A - acc[0]) * invJ;
-        rhs[1] = (Bx - acc[1]) * invJ;
-        rhs[2] = (By - acc[2]) * invJ;
-        rhs[3] = (Bz - acc[3]) * invJ;
-      } else {
-#pragma unroll
-        for (int m = 0; m < 6; ++m) {
-          float v = G[(3 * 6 + m) * NPS + p[3]];
-#pragma unroll
-          for (int f = 0; f < 3; ++f) v += G[(f * 6 + m) * NPS + p[f]];
-          rhs[m] = (v + acc[m]) * invJ;
-        }
+      for (int f = 0; f < 4; ++f) {
+        nxf[f] = g[12 + f];
+        nyf[f] = g[16 + f];
+        nzf[f] = g[20 + f];
       }
-      if (!stage) {
+      const float* G = sG + le * 4 * NCH * NPS;
 #pragma unroll
-        for (int m = 0; m < NF; ++m) P.rhs[((size_t)m * K + e0) * NP + item] = rhs[m];
-      } else {
+      for (int r = 0; r < GR; ++r) {
+        const int n = u + r * TPE;
+        if (n >= NP) continue;
+        const uint32_t pos = sGA[n].w;
+        const float4 lw = sLW[n];
+        const float lwf[4] = {lw.x, lw.y, lw.z, lw.w};
+        const int p[4] = {(int)(pos & 1023), (int)((pos >> 10) & 1023), (int)(pos >> 20), n};
+        float rhs[NF];
+        if constexpr (PHYS == BB_WAVE) {
+          // face order of src/BernsteinLift.jl:202-214: t=-1 face first, then f1, f2, f3
+          const float B3 = lwf[3] * G[(3 * 2 + 1) * NPS + p[3]];
+          float A = lwf[3] * G[(3 * 2 + 0) * NPS + p[3]];
+          float Bx = nxf[3] * B3, By = nyf[3] * B3, Bz = nzf[3] * B3;
 #pragma unroll
-        for (int m = 0; m < NF; ++m) {
-          const float r = fmaf(rkA, sRes[m * EPB * NP + item], dt * rhs[m]);
-          sRes[m * EPB * NP + item] = r;
-          sQ[m * EPB * NP + item] = fmaf(rkB, r, sQ[m * EPB * NP + item]);
+          for (int f = 0; f < 3; ++f) {
+            const float Bf = lwf[f] * G[(f * 2 + 1) * NPS + p[f]];
+            A = fmaf(lwf[f], G[(f * 2 + 0) * NPS + p[f]], A);
+            Bx = fmaf(nxf[f], Bf, Bx);
+            By = fmaf(nyf[f], Bf, By);
+            Bz = fmaf(nzf[f], Bf, Bz);
+          }
+          const float* vol = sVol + le * NP + n;
+          rhs[0] = (A - vol[0]) * invJ;
+          rhs[1] = (Bx - vol[EPB * NP]) * invJ;
+          rhs[2] = (By - vol[2 * EPB * NP]) * invJ;
+          rhs[3] = (Bz - vol[3 * EPB * NP]) * invJ;
+        } else {
+#pragma unroll
+          for (int m = 0; m < 6; ++m) {
+            float v = lwf[3] * G[(3 * 6 + m) * NPS + p[3]];
+#pragma unroll
+            for (int f = 0; f < 3; ++f) v = fmaf(lwf[f], G[(f * 6 + m) * NPS + p[f]], v);
+            rhs[m] = (v + sVol[(m * EPB + le) * NP + n]) * invJ;
+          }
+        }
+        const int item = le * NP + n;
+        if (!stage) {
+#pragma unroll
+          for (int m = 0; m < NF; ++m) P.rhs[((size_t)m * K + e0) * NP + item] = rhs[m];
+        } else {
+#pragma unroll
+          for (int m = 0; m < NF; ++m) {
+            const float rr = fmaf(rkA, sRes[m * EPB * NP + item], dt * rhs[m]);
+            sRes[m * EPB * NP + item] = rr;
+            sQ[m * EPB * NP + item] = fmaf(rkB, rr, sQ[m * EPB * NP + item]);
+          }
         }
       }
     }
@@ -509,17 +561,18 @@ __global__ void __launch_bounds__(NT) stage_fast_kernel(FastStageParams P) {
           issue_res(tnext);
         }
       }
-      if (P.trace_out) {
-        for (int item = tid; item < EPB * 4 * NFP; item += NT) {
-          const int le = item / (4 * NFP);
-          const int rem = item - le * 4 * NFP;
-          const int f = rem / NFP, a = rem - f * NFP;
-          const int64_t nbr = (int64_t)((uint32_t)sConn[le * 4 + f] >> 5);
-          if (nbr >= e0 && nbr < e0 + EPB) continue;
-          float* dst = P.trace_out + ((size_t)(e0 + le) * 4 + f) * NF * NFP + a;
-          const float* src = sQ + le * NP + sFvol[f * NFP + a];
+      if (P.trace_out && is_elem) {
+        const int64_t nbr = (int64_t)((uint32_t)sConn[le * 4 + ff] >> 5);
+        if (nbr < e0 || nbr >= e0 + EPB) {
+          float* dst0 = P.trace_out + ((size_t)(e0 + le) * 4 + ff) * NF * NFP;
 #pragma unroll
-          for (int m = 0; m < NF; ++m) dst[m * NFP] = src[m * EPB * NP];
+          for (int r = 0; r < FR; ++r) {
+            const int a = fa0 + r * FT;
+            if (a >= NFP) continue;
+            const float* src = sQ + le * NP + sFvol[ff * NFP + a];
+#pragma unroll
+            for (int m = 0; m < NF; ++m) dst0[m * NFP + a] = src[m * EPB * NP];
+          }
         }
       }
     }
@@ -533,42 +586,44 @@ __global__ void __launch_bounds__(NT) stage_fast_kernel(FastStageParams P) {
   if (tid == 0) tma_store_wait_all();
 }
 
-template <int N, int PHYS, int EPB, int NT>
+template <int N, int PHYS, int EPB, int TPE>
 int launch_fast_t(const FastLaunch& fl, const FastStageParams& P, cudaStream_t st) {
-  using L = FastLayout<N, PHYS, EPB>;
-  auto kern = stage_fast_kernel<N, PHYS, EPB, NT>;
+  using L = FastLayout<N, PHYS, EPB, TPE>;
+  auto kern = stage_fast_kernel<N, PHYS, EPB, TPE>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES) !=
       cudaSuccess)
     return BB_ERR_CUDA;
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, L::BYTES) != cudaSuccess ||
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, L::NT, L::BYTES) !=
+          cudaSuccess ||
       per_sm < 1)
     return BB_ERR_CUDA;
   if (P.K % EPB != 0) return BB_ERR_ARG;
   const int64_t ntiles = P.K / EPB;
   int64_t grid = (int64_t)per_sm * fl.num_sms;
   if (grid > ntiles) grid = ntiles;
-  kern<<<(int)grid, NT, L::BYTES, st>>>(P);
+  kern<<<(int)grid, L::NT, L::BYTES, st>>>(P);
   return cudaGetLastError() == cudaSuccess ? BB_OK : BB_ERR_CUDA;
 }
 
 }  // namespace
 
-// Registry of compiled (N, physics, EPB, threads) variants.
-#define BB_FAST_VARIANTS(X)  \
-  X(9, BB_WAVE, 4, 128)      \
-  X(9, BB_WAVE, 4, 256)      \
-  X(9, BB_WAVE, 2, 64)       \
-  X(9, BB_WAVE, 6, 192)      \
-  X(9, BB_MAXWELL, 2, 128)   \
-  X(9, BB_MAXWELL, 2, 256)
+// Registry of compiled (N, physics, elements per block, threads per element) variants.
+#define BB_FAST_VARIANTS(X) \
+  X(9, BB_WAVE, 4, 64)      \
+  X(9, BB_WAVE, 4, 32)      \
+  X(9, BB_WAVE, 2, 64)      \
+  X(9, BB_MAXWELL, 2, 64)   \
+  X(9, BB_MAXWELL, 2, 96)
 
+// The public tile description is (elements per block, threads per block).
 int bb_fast_find(int N, int physics, int epb, int threads, int64_t K) {
   int idx = 0;
-#define BB_FIND(n_, p_, e_, t_)                                                      \
-  if (N == n_ && physics == p_ && (epb == 0 || epb == e_) &&                         \
-      (threads == 0 || threads == t_) && (K <= 0 || K % e_ == 0))                     \
-    return idx;                                                                      \
+#define BB_FIND(n_, p_, e_, t_)                                                        \
+  if (N == n_ && physics == p_ && (epb == 0 || epb == e_) &&                           \
+      (threads == 0 || threads == FastLayout<n_, p_, e_, t_>::NT) &&                   \
+      (K <= 0 || K % e_ == 0))                                                         \
+    return idx;                                                                        \
   ++idx;
   BB_FAST_VARIANTS(BB_FIND)
 #undef BB_FIND
@@ -577,13 +632,13 @@ int bb_fast_find(int N, int physics, int epb, int threads, int64_t K) {
 
 int bb_fast_variant_info(int idx, int* epb, int* threads, size_t* smem) {
   int i = 0;
-#define BB_INFO(n_, p_, e_, t_)                              \
-  if (idx == i) {                                            \
-    *epb = e_;                                               \
-    *threads = t_;                                           \
-    *smem = FastLayout<n_, p_, e_>::BYTES;                   \
-    return BB_OK;                                            \
-  }                                                          \
+#define BB_INFO(n_, p_, e_, t_)                       \
+  if (idx == i) {                                     \
+    *epb = e_;                                        \
+    *threads = FastLayout<n_, p_, e_, t_>::NT;        \
+    *smem = FastLayout<n_, p_, e_, t_>::BYTES;        \
+    return BB_OK;                                     \
+  }                                                   \
   ++i;
   BB_FAST_VARIANTS(BB_INFO)
 #undef BB_INFO
@@ -592,8 +647,8 @@ int bb_fast_variant_info(int idx, int* epb, int* threads, size_t* smem) {
 
 int bb_fast_launch(int idx, const FastLaunch& fl, const FastStageParams& P, cudaStream_t st) {
   int i = 0;
-#define BB_LAUNCH(n_, p_, e_, t_)                                     \
-  if (idx == i) return launch_fast_t<n_, p_, e_, t_>(fl, P, st);      \
+#define BB_LAUNCH(n_, p_, e_, t_)                                 \
+  if (idx == i) return launch_fast_t<n_, p_, e_, t_>(fl, P, st);  \
   ++i;
   BB_FAST_VARIANTS(BB_LAUNCH)
 #undef BB_LAUNCH

@@ -161,8 +161,8 @@ def test_corrupt_connectivity_is_reported(cuda, bb):
     assert ei.value.status == 7
 
 
-FAST_TILES = {("wave", 9): [(4, 128), (4, 256), (2, 64), (6, 192)],
-              ("maxwell", 9): [(2, 128), (2, 256)]}
+FAST_TILES = {("wave", 9): [(4, 288), (4, 160), (2, 160)],
+              ("maxwell", 9): [(2, 192), (2, 256)]}
 
 
 def pulse_fields(nf):
