@@ -258,3 +258,59 @@ extern "C" int bb_mass_norms(bb_ctx* ctx, int N, int64_t K, int nf, int dtype, c
   }
   return finite ? BB_OK : bb_fail(ctx, BB_ERR_NONFINITE, "non-finite norm");
 }
+
+// -------------------------------------------------------------------------------------
+// bb_norms_noalloc: the same per-field sums without any allocation, for callers that must
+// not allocate device memory (code running while a CUDA graph is being captured on its
+// stream, runtimes whose device memory is owned by their own pool allocator, latency-bound
+// loops). Its partial sums live in a file-scope device array of fixed size that every GPU
+// loading this library holds until exit.
+// -------------------------------------------------------------------------------------
+namespace {
+
+constexpr int kNoAllocBlocks = 512;  // fixed grid of the partial-sum kernel
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocBlocks * kMaxFields * 3];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_partials on the current device, looked up once per device.
+// (In host code the array's name is only a host-side stand-in, not a device address.)
+int noalloc_scratch(double** out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices)
+    return BB_ERR_CUDA;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_partials) != cudaSuccess || !p) return BB_ERR_CUDA;
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return BB_OK;
+}
+
+}  // namespace
+
+extern "C" int bb_norms_noalloc(int N, int64_t K, int nf, int dtype, const void* a,
+                                const void* b, double* out_dev, void* stream) {
+  if (!valid_degree(N) || K < 0 || !valid_dtype(dtype) || !a || !out_dev) return BB_ERR_ARG;
+  if (nf < 1 || nf > kMaxFields) return BB_ERR_ARG;  // the scratch holds kMaxFields fields
+  double* part = nullptr;
+  int rc = noalloc_scratch(&part);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t n = K * np3(N);
+  // every block writes all of its partials before sum_rows reads them: nothing to clear
+  if (dtype == BB_F64)
+    norms_partial<double><<<kNoAllocBlocks, kRedThreads, 0, st>>>(n, nf, (const double*)a,
+                                                                  (const double*)b, part);
+  else
+    norms_partial<float><<<kNoAllocBlocks, kRedThreads, 0, st>>>(n, nf, (const float*)a,
+                                                                 (const float*)b, part);
+  if (cudaGetLastError() != cudaSuccess) return BB_ERR_CUDA;
+  sum_rows<<<1, kRedThreads, 0, st>>>(kNoAllocBlocks, nf * 3, part, out_dev);
+  if (cudaGetLastError() != cudaSuccess) return BB_ERR_CUDA;
+  return BB_OK;
+}

@@ -140,6 +140,19 @@ int bb_lsrk_run_host(bb_solver* s, double dt, int nsteps, const void* q_host_in,
 int bb_norms(bb_ctx* ctx, int N, int64_t K, int nf, int dtype, const void* a, const void* b,
              double* out_host, void* stream);
 
+/* The sums of bb_norms written to a caller-provided DEVICE buffer out_dev (3*nf doubles,
+ * same order), without allocating anything and without a context: for callers that must not
+ * allocate device memory -- code running while a CUDA graph is being captured on its stream,
+ * runtimes whose device memory belongs to their own pool allocator, latency-bound loops.
+ * No counterpart in the reference. Its scratch is a fixed file-scope device array
+ * (512 blocks x 8 fields x 3 doubles = 96 KiB) that every GPU loading this library keeps
+ * until exit; nf > 8 returns BB_ERR_ARG. The first call on a device looks up that array's
+ * device address (cudaGetSymbolAddress), so make it before any stream capture. All calls
+ * share the array: calls that overlap on the GPU (different streams, no ordering) race.
+ * Stream-ordered; does not synchronise. */
+int bb_norms_noalloc(int N, int64_t K, int nf, int dtype, const void* a, const void* b,
+                     double* out_dev, void* stream);
+
 /* Mass-matrix energy: out_host[f] = sum_e J_e (a_e^T M a_e) with M the Bernstein mass
  * matrix of the reference tetrahedron; with b != NULL the quadratic form of (a - b).
  * J is read from the geometry records (stride BB_GEO_STRIDE, solver dtype). */
