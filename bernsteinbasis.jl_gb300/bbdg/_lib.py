@@ -62,6 +62,21 @@ SIGNATURES = {
     "bb_norms_noalloc": (_I, [_I, _I64, _I, _I, _P, _P, _P, _P]),
 }
 
+class BatchProblem(ctypes.Structure):
+    """bb_batch_problem of include/bbdg.h."""
+    _fields_ = [("physics", ctypes.c_int), ("N", ctypes.c_int), ("K", ctypes.c_int64),
+                ("conn", ctypes.c_void_p), ("geo", ctypes.c_void_p), ("q", ctypes.c_void_p),
+                ("res", ctypes.c_void_p), ("dt", ctypes.c_double), ("tau", ctypes.c_double)]
+
+
+SIGNATURES.update({
+    "bb_batch_create": (_I, [_P, _I, ctypes.POINTER(BatchProblem), _I, ctypes.POINTER(_P)]),
+    "bb_batch_destroy": (_I, [_P]),
+    "bb_batch_set_tile": (_I, [_P, _I, _I, _I]),
+    "bb_batch_get_tile": (_I, [_P, _I, _I, ctypes.POINTER(_I)]),
+    "bb_batch_run": (_I, [_P, _I, _I, _P]),
+})
+
 _lib = None
 _lock = threading.Lock()
 

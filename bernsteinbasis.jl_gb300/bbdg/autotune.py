@@ -92,3 +92,49 @@ def tune(solver, steps: int = 3, use_cache: bool = True, verbose: bool = False):
     except OSError:
         pass
     return (kind, epb, nt), table
+
+
+BATCH_TILES = (1, 2, 4, 6, 8)
+
+
+def tune_batch(batch, steps: int = 2, verbose: bool = False):
+    """Per (physics, N) of a BatchSolver: time the generic stage tile sizes on the largest
+    problem of that kind and set the fastest for the batch. Returns {"physics N": {...}}."""
+    from .solver import DGSolver
+    table = {}
+    kinds = {}
+    for i, s in enumerate(batch.specs):
+        key = (s.physics, s.N)
+        if key not in kinds or batch.meshes[i].K > batch.meshes[kinds[key]].K:
+            kinds[key] = i
+    for (physics, N), i in sorted(kinds.items()):
+        spec = batch.specs[i]
+        solver = DGSolver(batch.meshes[i], N, physics, dtype=batch.dtype, tau=spec.tau,
+                          device=batch.device)
+        solver.set_kernel("generic")
+        q = torch.rand((solver.nf, solver.K, solver.Np), dtype=batch.dtype,
+                       device=batch.device) * 1e-3
+        r = torch.zeros_like(q)
+        times = {}
+        for epb in BATCH_TILES:
+            try:
+                solver.set_tile(epb, 256)
+            except Exception:
+                continue
+            solver.run(q, r, solver.dt_cfl(), 1, graph=False)
+            s0 = torch.cuda.Event(enable_timing=True)
+            s1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            s0.record()
+            solver.run(q, r, solver.dt_cfl(), steps, graph=False)
+            s1.record()
+            torch.cuda.synchronize()
+            times[epb] = s0.elapsed_time(s1) / steps
+        best = min(times, key=times.get)
+        batch.set_tile(physics, N, best)
+        table[f"{physics} N={N}"] = {"elems_per_block": best, "threads": 256,
+                                     "ms_per_step": times, "tuned_on_K": solver.K}
+        if verbose:
+            print(f"batch tile {physics} N={N}: {best} elements/block ({times})")
+        solver.close()
+    return table

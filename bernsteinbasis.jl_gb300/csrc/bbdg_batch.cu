@@ -1,0 +1,374 @@
+// Batched persistent stage kernel: many independent wave / Maxwell problems of uneven
+// degree N and element count K advance together, one launch per LSRK stage.
+//
+// Work items are (problem, element tile) pairs, numbered problem by problem; the blocks of a
+// persistent grid draw items from a device counter (one 64-bit atomicAdd per item, no
+// spinning) and run the generic stage tile (bbdg_stage_generic.cuh) for that problem,
+// reloading the degree tables into shared memory only when the problem changes. Each problem
+// keeps its own time step, tile shape (chosen per degree), trace buffers and state; a step
+// (5 stages + the counter reset) is replayed from a CUDA graph.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "bbdg_internal.cuh"
+#include "bbdg_stage_generic.cuh"
+
+namespace {
+
+constexpr int kBatchThreads = 256;
+const double kA[5] = {0.0, -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
+                      -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0};
+const double kB[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13612068292357.0,
+                      1720146321549.0 / 2090206949498.0, 3134564353537.0 / 4481467310338.0,
+                      2277821191437.0 / 14882151754819.0};
+
+template <class T>
+struct BatchDesc {
+  StageParams<T> P;      // rkA/rkB/trace pointers are filled in per stage by the kernel
+  T* trace[2];
+  int64_t tile_begin;    // first global work item of this problem
+  int physics;
+};
+
+template <class T>
+__global__ void __launch_bounds__(kBatchThreads)
+    batch_stage_kernel(const BatchDesc<T>* __restrict__ descs, int nprob, int64_t total,
+                       unsigned long long* counter, int par, T rkA, T rkB) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ long long s_item;
+  int cur = -1;
+  StageParams<T> P;
+  TileLayout L;
+  SmemTables st;
+  int phys = 0;
+  int64_t begin = 0;
+  while (true) {
+    __syncthreads();  // every thread is done with the previous tile (and its tables)
+    if (threadIdx.x == 0) s_item = (long long)atomicAdd(counter, 1ull);
+    __syncthreads();
+    const int64_t item = s_item;
+    if (item >= total) break;
+    int p = cur < 0 ? 0 : cur;
+    while (p + 1 < nprob && item >= descs[p + 1].tile_begin) ++p;
+    if (p != cur) {
+      const BatchDesc<T>& d = descs[p];
+      P = d.P;
+      P.rkA = rkA;
+      P.rkB = rkB;
+      P.trace_in = d.trace[par];
+      P.trace_out = d.trace[par ^ 1];
+      phys = d.physics;
+      begin = d.tile_begin;
+      const int NF = phys == BB_WAVE ? 4 : 6;
+      L = tile_layout_for(P.tab.N, NF, NF, sizeof(T), P.tab.nwords, P.epb);
+      st = load_tables(P.tab, P.gtab, reinterpret_cast<uint32_t*>(smem + L.tab_bytes));
+      T* sLj = reinterpret_cast<T*>(smem) + L.lj;
+      for (int j = threadIdx.x; j <= P.tab.N; j += blockDim.x) sLj[j] = P.lj[j];
+      cur = p;
+    }
+    if (phys == BB_WAVE)
+      generic_stage_tile<T, BB_WAVE>(P, L, st, item - begin);
+    else
+      generic_stage_tile<T, BB_MAXWELL>(P, L, st, item - begin);
+  }
+}
+
+template <class T, int NF>
+__global__ void batch_extract_kernel(DegTables tab, const uint32_t* __restrict__ gtab, int64_t K,
+                                     const T* __restrict__ q, T* __restrict__ tr) {
+  const int Np = tab.Np, Nfp = tab.Nfp;
+  const uint16_t* fvol = reinterpret_cast<const uint16_t*>(gtab + tab.o_fvol);
+  const int64_t total = K * 4 * NF * Nfp;
+  for (int64_t it = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; it < total;
+       it += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = it / (4 * NF * Nfp);
+    int rem = (int)(it - e * 4 * NF * Nfp);
+    const int f = rem / (NF * Nfp);
+    rem -= f * NF * Nfp;
+    const int fld = rem / Nfp, a = rem - fld * Nfp;
+    tr[it] = q[((size_t)fld * K + e) * Np + fvol[f * Nfp + a]];
+  }
+}
+
+}  // namespace
+
+struct bb_batch {
+  bb_ctx* ctx = nullptr;
+  int dtype = 0;
+  std::vector<bb_batch_problem> probs;
+  std::vector<const DegTables*> tabs;
+  std::vector<int> epb;          // per problem
+  std::vector<void*> trace;      // 2 per problem
+  void* d_desc = nullptr;
+  unsigned long long* d_counter = nullptr;  // 5 stage counters
+  int* d_status = nullptr;
+  int64_t total = 0;
+  size_t smem = 0;
+  int grid = 0;
+  bool dirty = true;             // descriptors need rebuilding
+  cudaStream_t cap = nullptr;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+};
+
+namespace {
+
+int batch_tile_default(int N, int nf, int dtype) {
+  // largest of 6, 4, 2, 1 elements whose generic tile fits in 100 KB of shared memory
+  const int cands[4] = {6, 4, 2, 1};
+  for (int e : cands) {
+    const TileLayout L = tile_layout_for(N, nf, nf, dtype_size(dtype), 1 << 12, e);
+    if (L.total <= 100 * 1024) return e;
+  }
+  return 1;
+}
+
+void drop_batch_graphs(bb_batch* b) {
+  for (auto& g : b->graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
+template <class T>
+int build_desc(bb_batch* b) {
+  bb_ctx* ctx = b->ctx;
+  const int np = (int)b->probs.size();
+  std::vector<BatchDesc<T>> h(np);
+  int64_t begin = 0;
+  size_t smem = 0;
+  for (int p = 0; p < np; ++p) {
+    const bb_batch_problem& pr = b->probs[p];
+    const DegTables* t = b->tabs[p];
+    BatchDesc<T>& d = h[p];
+    memset(&d, 0, sizeof(d));
+    d.P.tab = *t;
+    d.P.gtab = t->d_words;
+    d.P.lj = sizeof(T) == 8 ? (const T*)t->d_lj : (const T*)t->d_ljf;
+    d.P.K = pr.K;
+    d.P.epb = b->epb[p];
+    d.P.mode = 1;
+    d.P.dt = T(pr.dt);
+    d.P.tau = T(pr.tau);
+    d.P.q = (T*)pr.q;
+    d.P.res = (T*)pr.res;
+    d.P.geo = (const T*)pr.geo;
+    d.P.conn = pr.conn;
+    d.P.status = b->d_status;
+    d.trace[0] = (T*)b->trace[2 * p];
+    d.trace[1] = (T*)b->trace[2 * p + 1];
+    d.tile_begin = begin;
+    d.physics = pr.physics;
+    begin += (pr.K + b->epb[p] - 1) / b->epb[p];
+    const int nf = pr.physics == BB_WAVE ? 4 : 6;
+    const TileLayout L = tile_layout_for(pr.N, nf, nf, sizeof(T), t->nwords, b->epb[p]);
+    smem = std::max(smem, L.total);
+  }
+  if (smem > ctx->smem_optin) return bb_fail(ctx, BB_ERR_ARG, "batch tiles exceed shared memory");
+  if (!b->d_desc) {
+    BB_CUDA(ctx, cudaMalloc(&b->d_desc, sizeof(BatchDesc<T>) * np));
+  }
+  BB_CUDA(ctx, cudaMemcpy(b->d_desc, h.data(), sizeof(BatchDesc<T>) * np, cudaMemcpyHostToDevice));
+  b->total = begin;
+  b->smem = smem;
+  BB_CUDA(ctx, cudaFuncSetAttribute(batch_stage_kernel<T>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  BB_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_stage_kernel<T>,
+                                                             kBatchThreads, smem));
+  if (per_sm < 1) return bb_fail(ctx, BB_ERR_ARG, "batch tile does not fit on an SM");
+  b->grid = (int)std::min<int64_t>((int64_t)per_sm * ctx->num_sms, std::max<int64_t>(b->total, 1));
+  b->dirty = false;
+  return BB_OK;
+}
+
+template <class T>
+int enqueue_batch_step(bb_batch* b, int par, cudaStream_t st) {
+  BB_CUDA(b->ctx, cudaMemsetAsync(b->d_counter, 0, 5 * sizeof(unsigned long long), st));
+  for (int s = 0; s < 5; ++s) {
+    batch_stage_kernel<T><<<b->grid, kBatchThreads, b->smem, st>>>(
+        (const BatchDesc<T>*)b->d_desc, (int)b->probs.size(), b->total, b->d_counter + s,
+        (par + s) & 1, T(kA[s]), T(kB[s]));
+    int rc = bb_check_launch(b->ctx, "batch_stage_kernel");
+    if (rc) return rc;
+  }
+  return BB_OK;
+}
+
+template <class T>
+int batch_extract(bb_batch* b, cudaStream_t st) {
+  for (size_t p = 0; p < b->probs.size(); ++p) {
+    const bb_batch_problem& pr = b->probs[p];
+    const DegTables& t = *b->tabs[p];
+    const int nf = pr.physics == BB_WAVE ? 4 : 6;
+    int64_t grid = (pr.K * 4 * nf * t.Nfp + 255) / 256;
+    grid = std::min<int64_t>(std::max<int64_t>(grid, 1), (int64_t)b->ctx->num_sms * 8);
+    if (nf == 4)
+      batch_extract_kernel<T, 4><<<(int)grid, 256, 0, st>>>(t, t.d_words, pr.K, (const T*)pr.q,
+                                                            (T*)b->trace[2 * p]);
+    else
+      batch_extract_kernel<T, 6><<<(int)grid, 256, 0, st>>>(t, t.d_words, pr.K, (const T*)pr.q,
+                                                            (T*)b->trace[2 * p]);
+    int rc = bb_check_launch(b->ctx, "batch_extract_kernel");
+    if (rc) return rc;
+  }
+  return BB_OK;
+}
+
+template <class T>
+int batch_run_t(bb_batch* b, int nsteps, int use_graph, cudaStream_t st) {
+  bb_ctx* ctx = b->ctx;
+  if (b->dirty) {
+    drop_batch_graphs(b);
+    int rc = build_desc<T>(b);
+    if (rc) return rc;
+  }
+  int rc = batch_extract<T>(b, st);
+  if (rc) return rc;
+  if (!use_graph) {
+    for (int step = 0; step < nsteps; ++step) {
+      rc = enqueue_batch_step<T>(b, step & 1, st);
+      if (rc) return rc;
+    }
+  } else {
+    for (int par = 0; par < 2; ++par)
+      if (!b->graph[par]) {
+        cudaGraph_t g = nullptr;
+        BB_CUDA(ctx, cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
+        rc = enqueue_batch_step<T>(b, par, b->cap);
+        cudaError_t e = cudaStreamEndCapture(b->cap, &g);
+        if (rc) {
+          if (g) cudaGraphDestroy(g);
+          return rc;
+        }
+        if (e != cudaSuccess) return bb_fail(ctx, BB_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&b->graph[par], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return bb_fail(ctx, BB_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+      }
+    for (int step = 0; step < nsteps; ++step) {
+      BB_CUDA(ctx, cudaGraphLaunch(b->graph[step & 1], st));
+      ctx->launches += 5;
+    }
+  }
+  return BB_OK;
+}
+
+void free_batch(bb_batch* b) {
+  drop_batch_graphs(b);
+  for (void* p : b->trace) cudaFree(p);
+  cudaFree(b->d_desc);
+  cudaFree(b->d_counter);
+  cudaFree(b->d_status);
+  if (b->cap) cudaStreamDestroy(b->cap);
+  delete b;
+}
+
+}  // namespace
+
+extern "C" int bb_batch_create(bb_ctx* ctx, int nprob, const bb_batch_problem* probs, int dtype,
+                               bb_batch** out) {
+  if (!ctx || !out) return BB_ERR_ARG;
+  *out = nullptr;
+  if (nprob < 1 || !probs) return bb_fail(ctx, BB_ERR_ARG, "need at least one problem");
+  if (!valid_dtype(dtype)) return bb_fail(ctx, BB_ERR_ARG, "bad dtype");
+  int rc = bb_set_device(ctx);
+  if (rc) return rc;
+  bb_batch* b = new (std::nothrow) bb_batch();
+  if (!b) return BB_ERR_NOMEM;
+  b->ctx = ctx;
+  b->dtype = dtype;
+  for (int p = 0; p < nprob; ++p) {
+    const bb_batch_problem& pr = probs[p];
+    if ((pr.physics != BB_WAVE && pr.physics != BB_MAXWELL) || !valid_degree(pr.N) || pr.K < 1 ||
+        pr.K >= (int64_t(1) << 27) || !pr.conn || !pr.geo || !pr.q || !pr.res ||
+        !std::isfinite(pr.dt) || !std::isfinite(pr.tau)) {
+      free_batch(b);
+      return bb_fail(ctx, BB_ERR_ARG, "bad problem %d", p);
+    }
+    const DegTables* t = bb_tables(ctx, pr.N);
+    if (!t) {
+      free_batch(b);
+      return bb_fail(ctx, BB_ERR_NOMEM, "table allocation failed");
+    }
+    b->probs.push_back(pr);
+    b->tabs.push_back(t);
+    const int nf = pr.physics == BB_WAVE ? 4 : 6;
+    b->epb.push_back(batch_tile_default(pr.N, nf, dtype));
+    const size_t bytes = (size_t)pr.K * 4 * nf * t->Nfp * dtype_size(dtype);
+    for (int k = 0; k < 2; ++k) {
+      void* ptr = nullptr;
+      if (cudaMalloc(&ptr, bytes) != cudaSuccess) {
+        free_batch(b);
+        return bb_fail(ctx, BB_ERR_NOMEM, "trace allocation failed");
+      }
+      b->trace.push_back(ptr);
+    }
+  }
+  if (cudaMalloc(&b->d_counter, 5 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&b->d_status, sizeof(int)) != cudaSuccess ||
+      cudaMemset(b->d_status, 0, sizeof(int)) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking) != cudaSuccess) {
+    free_batch(b);
+    return bb_fail(ctx, BB_ERR_NOMEM, "batch allocation failed");
+  }
+  *out = b;
+  return BB_OK;
+}
+
+extern "C" int bb_batch_destroy(bb_batch* b) {
+  if (!b) return BB_ERR_ARG;
+  cudaSetDevice(b->ctx->device);
+  free_batch(b);
+  return BB_OK;
+}
+
+extern "C" int bb_batch_set_tile(bb_batch* b, int physics, int N, int elems_per_block) {
+  if (!b) return BB_ERR_ARG;
+  if (elems_per_block < 1 || elems_per_block > 64)
+    return bb_fail(b->ctx, BB_ERR_ARG, "elements per block must be 1..64");
+  const int nf = physics == BB_WAVE ? 4 : 6;
+  const TileLayout L = tile_layout_for(N, nf, nf, dtype_size(b->dtype), 1 << 12, elems_per_block);
+  if (L.total > b->ctx->smem_optin)
+    return bb_fail(b->ctx, BB_ERR_ARG, "tile of %d elements exceeds shared memory", elems_per_block);
+  int hits = 0;
+  for (size_t p = 0; p < b->probs.size(); ++p)
+    if (b->probs[p].physics == physics && b->probs[p].N == N) {
+      b->epb[p] = elems_per_block;
+      ++hits;
+    }
+  if (hits) b->dirty = true;
+  return BB_OK;
+}
+
+extern "C" int bb_batch_get_tile(const bb_batch* b, int physics, int N, int* elems_per_block) {
+  if (!b || !elems_per_block) return BB_ERR_ARG;
+  for (size_t p = 0; p < b->probs.size(); ++p)
+    if (b->probs[p].physics == physics && b->probs[p].N == N) {
+      *elems_per_block = b->epb[p];
+      return BB_OK;
+    }
+  return BB_ERR_ARG;
+}
+
+extern "C" int bb_batch_run(bb_batch* b, int nsteps, int use_graph, void* stream) {
+  if (!b) return BB_ERR_ARG;
+  if (nsteps < 0) return bb_fail(b->ctx, BB_ERR_ARG, "nsteps must be >= 0");
+  int rc = bb_set_device(b->ctx);
+  if (rc) return rc;
+  if (nsteps == 0) return BB_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  rc = b->dtype == BB_F64 ? batch_run_t<double>(b, nsteps, use_graph, st)
+                          : batch_run_t<float>(b, nsteps, use_graph, st);
+  if (rc) return rc;
+  int h = 0;
+  BB_CUDA(b->ctx, cudaMemcpyAsync(&h, b->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  BB_CUDA(b->ctx, cudaStreamSynchronize(st));
+  if (h) {
+    cudaMemsetAsync(b->d_status, 0, sizeof(int), st);
+    return bb_fail(b->ctx, BB_ERR_DEVICE, "device check failed (corrupt connectivity)");
+  }
+  return BB_OK;
+}

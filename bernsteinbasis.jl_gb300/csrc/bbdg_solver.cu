@@ -1,333 +1,28 @@
-// Fused DG right-hand side + low-storage RK stage for the wave and Maxwell examples.
-//
-// One thread block owns a tile of `epb` consecutive elements and does, per RK stage:
-//   1. stage q (all fields), geometry and connectivity of its tile in shared memory
-//   2. interface flux at every face node (examples/3d_wave.jl:41-56,
-//      examples/3d_maxwell.jl:185-209): the neighbour trace comes from shared memory when
-//      the neighbour is in the same tile, otherwise from the trace buffer written by the
-//      previous stage (only faces that cross a tile boundary are ever written or read)
-//   3. volume term (3d_wave.jl:59-79): the geometric combination of Dr, Ds, Dt is applied
-//      as sum_b alpha_b w(alpha - e_b), w(beta) = sum_a g_a x(beta + e_a), g the barycentric
-//      weights of the physical derivative (Dr = (D0 - D3)/2 etc.)
-//   4. lift of the four face fluxes (src/BernsteinLift.jl:139-220), accumulated in place
-//   5. divide by J, LSRK update res = A res + dt rhs, q += B res; write q, res and the
-//      tile's outgoing traces
-// q and res are updated in place: no block reads another tile's q, so there is no race.
+// DG solver object: fused right-hand side + low-storage RK stage for the wave and Maxwell
+// examples. The generic (runtime-degree) stage tile is in bbdg_stage_generic.cuh, the
+// degree-specialised FP32 kernels in bbdg_stage_fast.cu; this file owns trace buffers,
+// kernel selection, LSRK stepping and CUDA graphs.
 #include <cmath>
 #include <cstring>
 
 #include "bbdg_internal.cuh"
 #include "bbdg_stage_fast.cuh"
+#include "bbdg_stage_generic.cuh"
 
 namespace {
 
 constexpr int kThreads = 256;
 
-template <int PHYS>
-struct Phys;
-template <>
-struct Phys<BB_WAVE> {
-  static constexpr int NF = 4;  // p, u, v, w
-  static constexpr int NW = 4;  // div(u,v,w), dp/dx, dp/dy, dp/dz (scaled by J)
-  static constexpr float vol_sign = -1.f;
-};
-template <>
-struct Phys<BB_MAXWELL> {
-  static constexpr int NF = 6;  // Hx, Hy, Hz, Ex, Ey, Ez
-  static constexpr int NW = 6;  // curl terms
-  static constexpr float vol_sign = 1.f;
-};
-
-template <class T>
-struct StageParams {
-  DegTables tab;
-  const uint32_t* gtab;
-  const T* lj;
-  int64_t K;
-  int epb;
-  int mode;             // 0: write rhs to `rhs`; 1: LSRK stage update of q and res
-  T rkA, rkB, dt, tau;  // stage coefficients, time step, penalty (tau <= 0: as written)
-  T* q;                 // [NF][K][Np]
-  T* res;               // [NF][K][Np]
-  T* rhs;               // mode 0 output [NF][K][Np]
-  const T* trace_in;    // [K][4][NF][Nfp] or nullptr: gather neighbour traces from q
-  T* trace_out;         // [K][4][NF][Nfp] or nullptr
-  const T* geo;         // [K][BB_GEO_STRIDE]
-  const int32_t* conn;  // [K][4]
-  int* status;          // device error word
-};
-
-// Shared-memory layout of a tile (in units of T unless noted).
-struct TileLayout {
-  size_t q, out, flux, work, geo, lj, conn_bytes, tab_bytes, total;
-  int work_elems;
-};
-
-template <class T, int PHYS>
-TileLayout tile_layout(const DegTables& t, int epb) {
-  constexpr int NF = Phys<PHYS>::NF, NW = Phys<PHYS>::NW;
-  TileLayout L;
-  const size_t Np = t.Np, Nfp = t.Nfp, S = np2(t.N + 1);
-  size_t off = 0;
-  L.q = off; off += (size_t)NF * epb * Np;
-  L.out = off; off += (size_t)NF * epb * Np;
-  L.flux = off; off += (size_t)epb * 4 * NF * Nfp;
-  L.work = off;
-  const size_t wvol = (size_t)NW * epb * t.NpM1, wlift = 2 * (size_t)epb * NF * S;
-  L.work_elems = (int)(wvol > wlift ? wvol : wlift);
-  off += L.work_elems;
-  L.geo = off; off += (size_t)epb * BB_GEO_STRIDE;
-  L.lj = off; off += t.N + 1;
-  size_t bytes = align16(off * sizeof(T));
-  L.conn_bytes = bytes; bytes += align16((size_t)epb * 4 * sizeof(int32_t));
-  L.tab_bytes = bytes; bytes += (size_t)t.nwords * 4;
-  L.total = align16(bytes);
-  return L;
-}
-
 template <class T, int PHYS>
 __global__ void __launch_bounds__(kThreads) stage_kernel(StageParams<T> P, TileLayout L) {
-  constexpr int NF = Phys<PHYS>::NF, NW = Phys<PHYS>::NW;
   extern __shared__ __align__(16) unsigned char smem[];
-  T* sbase = reinterpret_cast<T*>(smem);
-  T* sQ = sbase + L.q;
-  T* sOut = sbase + L.out;
-  T* sFlux = sbase + L.flux;
-  T* sWork = sbase + L.work;
-  T* sGeo = sbase + L.geo;
-  T* sLj = sbase + L.lj;
-  int32_t* sConn = reinterpret_cast<int32_t*>(smem + L.conn_bytes);
   const SmemTables st =
       load_tables(P.tab, P.gtab, reinterpret_cast<uint32_t*>(smem + L.tab_bytes));
-  const int N = P.tab.N, Np = P.tab.Np, NpM1 = P.tab.NpM1, Nfp = P.tab.Nfp;
-  const int64_t K = P.K;
-  const int epb = P.epb;
-  for (int j = threadIdx.x; j <= N; j += blockDim.x) sLj[j] = P.lj[j];
-  const int64_t ntiles = (K + epb - 1) / epb;
-
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t e0 = tile * epb;
-    const int ne = (int)min64(epb, K - e0);
-    __syncthreads();
-    // ---- 1. stage q, geometry, connectivity --------------------------------------------
-    for (int fld = 0; fld < NF; ++fld)
-      copy_g2s(sQ + (size_t)fld * epb * Np, P.q + ((size_t)fld * K + e0) * Np, ne * Np);
-    copy_g2s(sGeo, P.geo + e0 * BB_GEO_STRIDE, ne * BB_GEO_STRIDE);
-    for (int t = threadIdx.x; t < ne * 4; t += blockDim.x) sConn[t] = __ldg(P.conn + e0 * 4 + t);
-    __syncthreads();
-
-    // ---- 2. interface flux -------------------------------------------------------------
-    for (int it = threadIdx.x; it < ne * 4 * Nfp; it += blockDim.x) {
-      const int le = it / (4 * Nfp);
-      const int rem = it - le * 4 * Nfp;
-      const int f = rem / Nfp, a = rem - f * Nfp;
-      const int32_t c = sConn[le * 4 + f];
-      const int64_t nbr = (int64_t)((uint32_t)c >> 5);
-      const int nface = (c >> 3) & 3, o = c & 7;
-      T d[NF];
-      const int vM = st.fvol[f * Nfp + a];
-      if (nbr >= K || o > 5) {
-        atomicOr(P.status, 1);
-        for (int fld = 0; fld < NF; ++fld) d[fld] = T(0);
-      } else {
-        const int ap = st.fperm[o * Nfp + a];
-        if (nbr >= e0 && nbr < e0 + ne) {
-          const int vP = st.fvol[nface * Nfp + ap];
-          const T* qP = sQ + (size_t)(nbr - e0) * Np + vP;
-          const T* qM = sQ + (size_t)le * Np + vM;
-#pragma unroll
-          for (int fld = 0; fld < NF; ++fld) d[fld] = qP[(size_t)fld * epb * Np] - qM[(size_t)fld * epb * Np];
-        } else if (P.trace_in) {
-          const T* tp = P.trace_in + ((size_t)nbr * 4 + nface) * NF * Nfp + ap;
-          const T* qM = sQ + (size_t)le * Np + vM;
-#pragma unroll
-          for (int fld = 0; fld < NF; ++fld) d[fld] = __ldg(tp + (size_t)fld * Nfp) - qM[(size_t)fld * epb * Np];
-        } else {
-          const int vP = st.fvol[nface * Nfp + ap];
-          const T* qP = P.q + (size_t)nbr * Np + vP;
-          const T* qM = sQ + (size_t)le * Np + vM;
-#pragma unroll
-          for (int fld = 0; fld < NF; ++fld) d[fld] = __ldg(qP + (size_t)fld * K * Np) - qM[(size_t)fld * epb * Np];
-        }
-      }
-      const T* g = sGeo + le * BB_GEO_STRIDE;
-      const T nx = g[12 + f], ny = g[16 + f], nz = g[20 + f];
-      T cp = T(1), cu = T(1);
-      if (P.tau > T(0)) {
-        const T Jf = sqrt(nx * nx + ny * ny + nz * nz);
-        cp = P.tau * Jf;
-        cu = P.tau / Jf;
-      }
-      T fl[NF];
-      if constexpr (PHYS == BB_WAVE) {
-        // 3d_wave.jl:45-54
-        const T ndotdU = nx * d[1] + ny * d[2] + nz * d[3];
-        const T A = cp * d[0] - ndotdU;
-        const T B = cu * ndotdU - d[0];
-        fl[0] = T(0.5) * A;
-        fl[1] = T(0.5) * (B * nx);
-        fl[2] = T(0.5) * (B * ny);
-        fl[3] = T(0.5) * (B * nz);
-      } else {
-        // 3d_maxwell.jl:189-207: 0.5 (fx nx + fy ny + fz nz)(du) + 0.5 du - 0.5 n (n.d)
-        const T Hx = d[0], Hy = d[1], Hz = d[2], Ex = d[3], Ey = d[4], Ez = d[5];
-        const T ndH = nx * Hx + ny * Hy + nz * Hz;
-        const T ndE = nx * Ex + ny * Ey + nz * Ez;
-        const T ax[6] = {T(0), Ez, -Ey, T(0), -Hz, Hy};
-        const T ay[6] = {-Ez, T(0), Ex, Hz, T(0), -Hx};
-        const T az[6] = {Ey, -Ex, T(0), -Hy, Hx, T(0)};
-        const T nd[6] = {ndH * nx, ndH * ny, ndH * nz, ndE * nx, ndE * ny, ndE * nz};
-#pragma unroll
-        for (int m = 0; m < 6; ++m)
-          fl[m] = T(0.5) * ax[m] * nx + T(0.5) * ay[m] * ny + T(0.5) * az[m] * nz +
-                  T(0.5) * (cp * d[m]) - T(0.5) * (cu * nd[m]);
-      }
-      T* fo = sFlux + ((size_t)(le * 4 + f) * NF) * Nfp + a;
-#pragma unroll
-      for (int fld = 0; fld < NF; ++fld) fo[(size_t)fld * Nfp] = fl[fld];
-    }
-
-    // ---- 3a. volume term at degree N-1 -------------------------------------------------
-    for (int it = threadIdx.x; it < ne * NpM1; it += blockDim.x) {
-      const int le = it / NpM1, b = it - le * NpM1;
-      const uint32_t c = st.node3m1[b];
-      const int i = c & 0xff, j = (c >> 8) & 0xff, k = c >> 16;
-      const int idx[4] = {ijk3(N, i + 1, j, k), ijk3(N, i, j + 1, k), ijk3(N, i, j, k + 1),
-                          ijk3(N, i, j, k)};
-      const T* g = sGeo + le * BB_GEO_STRIDE;
-      // barycentric weights of d/dx, d/dy, d/dz (times J): g_a = (rxJ, sxJ, txJ, -sum)/2;
-      // the fourth weight is implied by the differences below
-      T gx[3], gy[3], gz[3];
-      gx[0] = T(0.5) * g[0]; gx[1] = T(0.5) * g[1]; gx[2] = T(0.5) * g[2];
-      gy[0] = T(0.5) * g[3]; gy[1] = T(0.5) * g[4]; gy[2] = T(0.5) * g[5];
-      gz[0] = T(0.5) * g[6]; gz[1] = T(0.5) * g[7]; gz[2] = T(0.5) * g[8];
-      const T* q0 = sQ + (size_t)le * Np;
-      auto F = [&](int fld, int a) { return q0[(size_t)fld * epb * Np + idx[a]]; };
-      T w[NW];
-#pragma unroll
-      for (int m = 0; m < NW; ++m) w[m] = T(0);
-      // sum_a g_a x(beta+e_a) with sum_a g_a = 0, formed as sum_{a<3} g_a (x_a - x_3) so
-      // that smooth data cancels in the differences (as the reference's Dr = (D0 - D3)/2)
-      if constexpr (PHYS == BB_WAVE) {
-        const T p3 = F(0, 3), u3 = F(1, 3), v3 = F(2, 3), w3 = F(3, 3);
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          const T p = F(0, a) - p3, u = F(1, a) - u3, v = F(2, a) - v3, ww = F(3, a) - w3;
-          w[0] += gx[a] * u + gy[a] * v + gz[a] * ww;
-          w[1] += gx[a] * p;
-          w[2] += gy[a] * p;
-          w[3] += gz[a] * p;
-        }
-      } else {
-        const T Hx3 = F(0, 3), Hy3 = F(1, 3), Hz3 = F(2, 3);
-        const T Ex3 = F(3, 3), Ey3 = F(4, 3), Ez3 = F(5, 3);
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          const T Hx = F(0, a) - Hx3, Hy = F(1, a) - Hy3, Hz = F(2, a) - Hz3;
-          const T Ex = F(3, a) - Ex3, Ey = F(4, a) - Ey3, Ez = F(5, a) - Ez3;
-          w[0] += -gy[a] * Ez + gz[a] * Ey;  // d/dt Hx = -dEz/dy + dEy/dz
-          w[1] += gx[a] * Ez - gz[a] * Ex;   // d/dt Hy
-          w[2] += -gx[a] * Ey + gy[a] * Ex;  // d/dt Hz
-          w[3] += gy[a] * Hz - gz[a] * Hy;   // d/dt Ex
-          w[4] += -gx[a] * Hz + gz[a] * Hx;  // d/dt Ey
-          w[5] += gx[a] * Hy - gy[a] * Hx;   // d/dt Ez
-        }
-      }
-#pragma unroll
-      for (int m = 0; m < NW; ++m) sWork[((size_t)m * epb + le) * NpM1 + b] = w[m];
-    }
-    __syncthreads();
-    // ---- 3b. elevate back to degree N: out(alpha) = sign * sum_b alpha_b w(alpha - e_b) -
-    for (int it = threadIdx.x; it < ne * Np; it += blockDim.x) {
-      const int le = it / Np, n = it - le * Np;
-      const uint32_t c = st.node3[n];
-      const int i = c & 0xff, j = (c >> 8) & 0xff, k = c >> 16, l = N - i - j - k;
-      T acc[NW];
-#pragma unroll
-      for (int m = 0; m < NW; ++m) acc[m] = T(0);
-      const T* wb = sWork + (size_t)le * NpM1;
-      const size_t ws = (size_t)epb * NpM1;
-      if (i > 0) {
-        const int x = ijk3(N - 1, i - 1, j, k);
-#pragma unroll
-        for (int m = 0; m < NW; ++m) acc[m] += T(i) * wb[m * ws + x];
-      }
-      if (j > 0) {
-        const int x = ijk3(N - 1, i, j - 1, k);
-#pragma unroll
-        for (int m = 0; m < NW; ++m) acc[m] += T(j) * wb[m * ws + x];
-      }
-      if (k > 0) {
-        const int x = ijk3(N - 1, i, j, k - 1);
-#pragma unroll
-        for (int m = 0; m < NW; ++m) acc[m] += T(k) * wb[m * ws + x];
-      }
-      if (l > 0) {
-        const int x = ijk3(N - 1, i, j, k);
-#pragma unroll
-        for (int m = 0; m < NW; ++m) acc[m] += T(l) * wb[m * ws + x];
-      }
-#pragma unroll
-      for (int m = 0; m < NF; ++m)
-        sOut[((size_t)m * epb + le) * Np + n] = T(Phys<PHYS>::vol_sign) * acc[m];
-    }
-    __syncthreads();
-
-    // ---- 4. lift of the face fluxes, face t=-1 first as src/BernsteinLift.jl:202-205 ----
-    {
-      const int order[4] = {3, 0, 1, 2};
-      const int S = np2(N + 1);
-      T* bufA = sWork;
-      T* bufB = sWork + (size_t)epb * NF * S;
-      for (int q = 0; q < 4; ++q) {
-        const int f = order[q];
-        lift_face_accumulate<T>(N, f, ne, NF, st.node2, sFlux + (size_t)f * NF * Nfp,
-                                4 * NF * Nfp, Nfp, sOut, Np, epb * Np, bufA, bufB, sLj);
-      }
-    }
-
-    // ---- 5. divide by J, RK update, write back -----------------------------------------
-    if (P.mode == 0) {
-      for (int fld = 0; fld < NF; ++fld) {
-        T* dst = P.rhs + ((size_t)fld * K + e0) * Np;
-        const T* src = sOut + (size_t)fld * epb * Np;
-        for (int t = threadIdx.x; t < ne * Np; t += blockDim.x) {
-          const int le = t / Np;
-          dst[t] = src[t] * sGeo[le * BB_GEO_STRIDE + 9];
-        }
-      }
-    } else {
-      for (int fld = 0; fld < NF; ++fld) {
-        T* gq = P.q + ((size_t)fld * K + e0) * Np;
-        T* gr = P.res + ((size_t)fld * K + e0) * Np;
-        T* sq = sQ + (size_t)fld * epb * Np;
-        const T* so = sOut + (size_t)fld * epb * Np;
-        for (int t = threadIdx.x; t < ne * Np; t += blockDim.x) {
-          const int le = t / Np;
-          const T rhs = so[t] * sGeo[le * BB_GEO_STRIDE + 9];
-          const T r = P.rkA * gr[t] + P.dt * rhs;
-          const T qn = sq[t] + P.rkB * r;
-          gr[t] = r;
-          gq[t] = qn;
-          sq[t] = qn;
-        }
-      }
-      if (P.trace_out) {
-        __syncthreads();
-        for (int it = threadIdx.x; it < ne * 4 * NF * Nfp; it += blockDim.x) {
-          const int le = it / (4 * NF * Nfp);
-          int rem = it - le * 4 * NF * Nfp;
-          const int f = rem / (NF * Nfp);
-          rem -= f * NF * Nfp;
-          const int fld = rem / Nfp, a = rem - fld * Nfp;
-          const int64_t nbr = (int64_t)((uint32_t)sConn[le * 4 + f] >> 5);
-          if (nbr >= e0 && nbr < e0 + ne) continue;  // neighbour inside the tile
-          P.trace_out[((size_t)(e0 + le) * 4 + f) * NF * Nfp + (size_t)fld * Nfp + a] =
-              sQ[((size_t)fld * epb + le) * Np + st.fvol[f * Nfp + a]];
-        }
-      }
-    }
-  }
+  T* sLj = reinterpret_cast<T*>(smem) + L.lj;
+  for (int j = threadIdx.x; j <= P.tab.N; j += blockDim.x) sLj[j] = P.lj[j];
+  const int64_t ntiles = (P.K + P.epb - 1) / P.epb;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+    generic_stage_tile<T, PHYS>(P, L, st, tile);
 }
 
 // Writes every face trace of q (all faces) into the trace buffer.

@@ -131,6 +131,36 @@ int bb_lsrk_run_host(bb_solver* s, double dt, int nsteps, const void* q_host_in,
                      void* q_host_out, void* q_dev, void* res_dev, int use_graph,
                      void* stream);
 
+/* ---- batched uneven solves ------------------------------------------------------------
+ * Many independent wave / Maxwell problems of different degree N and element count K advance
+ * together: one persistent launch per LSRK stage whose blocks draw (problem, element tile)
+ * work items from a device counter, each step replayed from a CUDA graph. Each problem keeps
+ * its own time step and penalty; the tile shape is chosen per (physics, N). No counterpart in
+ * the reference, which solves one problem per script (examples/3d_wave.jl,
+ * examples/3d_maxwell.jl). Arrays are device pointers in the batch dtype and must outlive
+ * the batch object. */
+typedef struct {
+  int physics;          /* BB_WAVE or BB_MAXWELL */
+  int N;                /* degree, 1..BB_MAX_DEGREE */
+  int64_t K;            /* elements */
+  const int32_t* conn;  /* K*4 packed connectivity (as bb_solver_create) */
+  const void* geo;      /* K*BB_GEO_STRIDE geometry records */
+  void* q;              /* [nf][K][Np] state, updated in place */
+  void* res;            /* [nf][K][Np] LSRK register */
+  double dt;            /* this problem's time step */
+  double tau;           /* penalty mode, as bb_solver_create */
+} bb_batch_problem;
+
+typedef struct bb_batch bb_batch;
+int bb_batch_create(bb_ctx* ctx, int nprob, const bb_batch_problem* probs, int dtype,
+                    bb_batch** out);
+int bb_batch_destroy(bb_batch* b);
+/* Elements per work item for every problem with this physics and degree. */
+int bb_batch_set_tile(bb_batch* b, int physics, int N, int elems_per_block);
+int bb_batch_get_tile(const bb_batch* b, int physics, int N, int* elems_per_block);
+/* nsteps LSRK steps of every problem; synchronises the stream to check device status. */
+int bb_batch_run(bb_batch* b, int nsteps, int use_graph, void* stream);
+
 /* ---- reductions (FP64 accumulation, warp-shuffle trees) ------------------------------ */
 
 /* For each field f of nf fields laid out as [nf][K][Np]:

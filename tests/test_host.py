@@ -109,3 +109,11 @@ def test_face_node_tables_agree_with_oracle_fmask(bb):
 def test_product_rejects_bad_degree(bb):
     with pytest.raises(ValueError):
         bb.mesh.uniform_tet_mesh(1)
+
+
+def test_config4_problem_set_is_seeded_and_in_range():
+    from bbdg.batch import config4_problems
+    a, b = config4_problems(), config4_problems()
+    assert len(a) == 48 and a == b
+    assert all(4 <= s.N <= 11 and 4 <= s.n <= 20 for s in a)
+    assert {s.physics for s in a} == {"wave", "maxwell"}
