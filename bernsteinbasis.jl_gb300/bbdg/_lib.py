@@ -60,6 +60,7 @@ SIGNATURES = {
     "bb_norms": (_I, [_P, _I, _I64, _I, _I, _P, _P, ctypes.POINTER(_D), _P]),
     "bb_mass_norms": (_I, [_P, _I, _I64, _I, _I, _P, _P, _P, ctypes.POINTER(_D), _P]),
     "bb_norms_noalloc": (_I, [_I, _I64, _I, _I, _P, _P, _P, _P]),
+    "bb_project": (_I, [_P, _I, _I, _I64, _I, _I, _P, _I, _P, _P]),
 }
 
 class BatchProblem(ctypes.Structure):

@@ -33,45 +33,55 @@ struct BatchDesc {
 };
 
 template <class T>
-__global__ void __launch_bounds__(kBatchThreads)
+__global__ void __launch_bounds__(kBatchThreads, 3)
     batch_stage_kernel(const BatchDesc<T>* __restrict__ descs, int nprob, int64_t total,
                        unsigned long long* counter, int par, T rkA, T rkB) {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ long long s_item;
-  int cur = -1;
-  StageParams<T> P;
-  TileLayout L;
-  SmemTables st;
-  int phys = 0;
-  int64_t begin = 0;
+  // the current problem's parameters live in shared memory, not in registers
+  __shared__ StageParams<T> sP;
+  __shared__ TileLayout sL;
+  __shared__ long long s_item, s_begin;
+  __shared__ int s_prob, s_phys, s_reload;
+  if (threadIdx.x == 0) s_prob = -1;
   while (true) {
     __syncthreads();  // every thread is done with the previous tile (and its tables)
-    if (threadIdx.x == 0) s_item = (long long)atomicAdd(counter, 1ull);
+    if (threadIdx.x == 0) {
+      const long long item = (long long)atomicAdd(counter, 1ull);
+      s_item = item;
+      s_reload = 0;
+      if (item < total) {
+        int p = s_prob < 0 ? 0 : s_prob;  // items only grow, so the problem index only grows
+        while (p + 1 < nprob && item >= descs[p + 1].tile_begin) ++p;
+        if (p != s_prob) {
+          const BatchDesc<T>& d = descs[p];
+          sP = d.P;
+          sP.rkA = rkA;
+          sP.rkB = rkB;
+          sP.trace_in = d.trace[par];
+          sP.trace_out = d.trace[par ^ 1];
+          s_phys = d.physics;
+          s_begin = d.tile_begin;
+          const int NF = d.physics == BB_WAVE ? 4 : 6;
+          sL = tile_layout_for(d.P.tab.N, NF, NF, sizeof(T), d.P.tab.nwords, d.P.epb);
+          s_prob = p;
+          s_reload = 1;
+        }
+      }
+    }
     __syncthreads();
     const int64_t item = s_item;
     if (item >= total) break;
-    int p = cur < 0 ? 0 : cur;
-    while (p + 1 < nprob && item >= descs[p + 1].tile_begin) ++p;
-    if (p != cur) {
-      const BatchDesc<T>& d = descs[p];
-      P = d.P;
-      P.rkA = rkA;
-      P.rkB = rkB;
-      P.trace_in = d.trace[par];
-      P.trace_out = d.trace[par ^ 1];
-      phys = d.physics;
-      begin = d.tile_begin;
-      const int NF = phys == BB_WAVE ? 4 : 6;
-      L = tile_layout_for(P.tab.N, NF, NF, sizeof(T), P.tab.nwords, P.epb);
-      st = load_tables(P.tab, P.gtab, reinterpret_cast<uint32_t*>(smem + L.tab_bytes));
-      T* sLj = reinterpret_cast<T*>(smem) + L.lj;
-      for (int j = threadIdx.x; j <= P.tab.N; j += blockDim.x) sLj[j] = P.lj[j];
-      cur = p;
+    uint32_t* stab = reinterpret_cast<uint32_t*>(smem + sL.tab_bytes);
+    if (s_reload) {
+      load_tables(sP.tab, sP.gtab, stab);
+      T* sLj = reinterpret_cast<T*>(smem) + sL.lj;
+      for (int j = threadIdx.x; j <= sP.tab.N; j += blockDim.x) sLj[j] = sP.lj[j];
     }
-    if (phys == BB_WAVE)
-      generic_stage_tile<T, BB_WAVE>(P, L, st, item - begin);
+    const SmemTables st = tables_view(sP.tab, stab);
+    if (s_phys == BB_WAVE)
+      generic_stage_tile<T, BB_WAVE>(sP, sL, st, item - s_begin);  // starts with a barrier
     else
-      generic_stage_tile<T, BB_MAXWELL>(P, L, st, item - begin);
+      generic_stage_tile<T, BB_MAXWELL>(sP, sL, st, item - s_begin);
   }
 }
 

@@ -117,6 +117,17 @@ struct SmemTables {
   const uint16_t* fperm;
 };
 
+// Shared-memory view of tables already copied to `s`.
+__device__ __forceinline__ SmemTables tables_view(const DegTables& t, const uint32_t* s) {
+  SmemTables r;
+  r.node3 = s + t.o_node3;
+  r.node3m1 = s + t.o_node3m1;
+  r.node2 = reinterpret_cast<const uint16_t*>(s + t.o_node2);
+  r.fvol = reinterpret_cast<const uint16_t*>(s + t.o_fvol);
+  r.fperm = reinterpret_cast<const uint16_t*>(s + t.o_fperm);
+  return r;
+}
+
 // Copies `words` 32-bit words of tables into shared memory (all threads participate).
 __device__ __forceinline__ SmemTables load_tables(const DegTables& t, const uint32_t* g,
                                                   uint32_t* s) {

@@ -131,6 +131,14 @@ int bb_lsrk_run_host(bb_solver* s, double dt, int nsteps, const void* q_host_in,
                      void* q_host_out, void* q_dev, void* res_dev, int use_graph,
                      void* stream);
 
+/* ---- degree reduction --------------------------------------------------------------
+ * FP64 L2 projection of degree-N Bernstein coefficients to degree M < N, per element and
+ * field: c_M = M_MM^{-1} E_{M->N}^T M_NN c_N (Bernstein mass matrices of the reference
+ * tetrahedron, E the degree elevation). in: [nf][K][Np(N)], out: [nf][K][Np(M)]; either
+ * may be FP32 or FP64, arithmetic is FP64. No counterpart in the reference. */
+int bb_project(bb_ctx* ctx, int N, int M, int64_t K, int nf, int dtype_in, const void* in,
+               int dtype_out, void* out, void* stream);
+
 /* ---- batched uneven solves ------------------------------------------------------------
  * Many independent wave / Maxwell problems of different degree N and element count K advance
  * together: one persistent launch per LSRK stage whose blocks draw (problem, element tile)

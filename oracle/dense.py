@@ -194,6 +194,24 @@ def deriv_from_vandermonde(N, seed=0):
     return [np.linalg.solve(V, (Vd - Vl) / 2) for Vd in (Vi, Vj, Vk)]
 
 
+def elevation3_dense(M, N):
+    """3D degree elevation E (Np(N) x Np(M)): B^M_a = sum_g E[g, a] B^N_g."""
+    LM, LN = lut3(M), lut3(N)
+    E = np.zeros((len(LN), len(LM)))
+    for a, al in enumerate(LM):
+        for g, ga in enumerate(LN):
+            d = tuple(x - y for x, y in zip(ga, al))
+            if min(d) >= 0:
+                E[g, a] = _multinom(al) * _multinom(d) / _multinom(ga)
+    return E
+
+
+def projection_dense(N, M):
+    """L2 projection from degree N to M: P = M_MM^{-1} E_{M->N}^T M_NN (Np(M) x Np(N))."""
+    E = elevation3_dense(M, N)
+    return np.linalg.solve(np.array(mass(M)), E.T @ np.array(mass(N)))
+
+
 def to_float(M):
     return np.array([[float(v) for v in row] for row in M], dtype=np.float64)
 

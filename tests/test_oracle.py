@@ -176,3 +176,16 @@ def test_example_analytic_solution(oracle_cpu, bb, phys, tau):
     u = np.einsum("pn,fkn->fkp", V, qT)
     err = max(np.abs(u[i] - ex[i]).max() for i in range(len(ex)))
     assert err < 5e-4, err
+
+
+def test_projection_operator_definition():
+    """P = M_MM^-1 E^T M_NN reproduces degree-M polynomials and is the L2-orthogonal map."""
+    for N, M in ((3, 2), (5, 3), (10, 5)):
+        P = dense.projection_dense(N, M)
+        E = dense.elevation3_dense(M, N)
+        assert np.allclose(P @ E, np.eye(P.shape[0]), atol=1e-10)     # exact on degree M
+        MN = np.array(dense.mass(N))
+        rng = np.random.default_rng(N)
+        c = rng.standard_normal(MN.shape[0])
+        r = c - E @ (P @ c)                                           # residual is orthogonal
+        assert np.abs(E.T @ MN @ r).max() < 1e-10 * np.abs(c).max()
