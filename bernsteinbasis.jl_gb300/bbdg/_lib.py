@@ -76,6 +76,22 @@ SIGNATURES.update({
     "bb_batch_set_tile": (_I, [_P, _I, _I, _I]),
     "bb_batch_get_tile": (_I, [_P, _I, _I, ctypes.POINTER(_I)]),
     "bb_batch_run": (_I, [_P, _I, _I, _P]),
+    "bb_gemm_bf16": (_I, [_P, _I64, _I, _I, _P, _P, ctypes.c_float, _P, _I, _P, _P, _P, _P, _P,
+                          _I, _I, _P]),
+    "bb_device_status": (_I, [_P, _P, ctypes.POINTER(_I)]),
+    "bb_transpose_bf16": (_I, [_P, _I64, _I, _P, _P, _P]),
+    "bb_mlp_create": (_I, [_P, _I, _I, _I, _I, _I64, ctypes.c_uint64, ctypes.POINTER(_P)]),
+    "bb_mlp_destroy": (_I, [_P]),
+    "bb_mlp_num_params": (_I64, [_P]),
+    "bb_mlp_set_params": (_I, [_P, _P, _P]),
+    "bb_mlp_get_params": (_I, [_P, _P, _P]),
+    "bb_mlp_get_grads": (_I, [_P, _P, _P]),
+    "bb_mlp_fwd": (_I, [_P, _I64, _P, _P, _P, _I, _P]),
+    "bb_mlp_bwd": (_I, [_P, _I64, _P, _P, _P, _P]),
+    "bb_mlp_step": (_I, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                         _P]),
+    "bb_closure_features": (_I, [_P, _I, _I64, _I, _P, _I, _P, ctypes.c_float, _P, _P, _P]),
+    "bb_closure_apply": (_I, [_P, _I, _I64, _I, _I, ctypes.c_float, _P, _P, _P]),
 })
 
 _lib = None

@@ -86,6 +86,7 @@ struct bb_ctx {
   double* d_red = nullptr;     // reduction scratch (FP64 partials)
   size_t red_cap = 0;          // entries
   double* h_red = nullptr;     // pinned host mirror
+  int* d_status = nullptr;     // device error word of the GEMM / closure kernels
 };
 
 // Error helpers -----------------------------------------------------------------------
@@ -99,6 +100,8 @@ int bb_fail(bb_ctx* ctx, int code, const char* fmt, ...);
 
 // Builds (or returns the cached) tables of degree N. Returns nullptr on failure.
 const DegTables* bb_tables(bb_ctx* ctx, int N);
+// The context's device error word (allocated on first use; nullptr on failure).
+int* bb_ctx_status_word(bb_ctx* ctx);
 // Makes the context's device current.
 int bb_set_device(bb_ctx* ctx);
 // Checks a launch and counts it.

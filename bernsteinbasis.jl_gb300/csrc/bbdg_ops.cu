@@ -74,6 +74,7 @@ extern "C" int bb_ctx_destroy(bb_ctx* ctx) {
   for (auto& t : ctx->tabs) free_tables(t);
   cudaFree(ctx->d_red);
   cudaFreeHost(ctx->h_red);
+  cudaFree(ctx->d_status);
   delete ctx;
   return BB_OK;
 }

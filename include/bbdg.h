@@ -197,6 +197,62 @@ int bb_norms_noalloc(int N, int64_t K, int nf, int dtype, const void* a, const v
 int bb_mass_norms(bb_ctx* ctx, int N, int64_t K, int nf, int dtype, const void* a,
                   const void* b, const void* geo, double* out_host, void* stream);
 
+/* ---- learned per-element closure: BF16 tensor-core GEMM and MLP ---------------------
+ * No counterpart in the reference. Matrices are row-major device arrays. */
+
+/* C = alpha * A[M x K] * B[N x K]^T on the tensor cores (BF16 operands, FP32 accumulation),
+ * then, per output element v (row r, column c):
+ *   v += bias[c];  act 1: pre[r][c] = v (if pre), v = GELU(v);  act 2: v *= GELU'(pre[r][c])
+ *   C_f32[r][c] = v; C_bf16[r][c] = bf16(v); CT_bf16[c][r] = bf16(v); bias_grad[c] += sum_r v
+ * (every output optional, at least one given). A, B 16-byte aligned, K % 8 == 0; row-major
+ * outputs use ldc >= N, the transposed one ldt >= M. Stream-ordered; a pipeline wait that runs
+ * out sets the context's device status word (bb_device_status). */
+int bb_gemm_bf16(bb_ctx* ctx, int64_t M, int N, int K, const void* A, const void* B,
+                 float alpha, const float* bias, int act, float* pre, float* C_f32,
+                 void* C_bf16, void* CT_bf16, float* bias_grad, int ldc, int ldt, void* stream);
+
+/* Reads and clears the context's device status word (synchronises the stream); *out = 0 when
+ * no kernel reported a problem, bit 0 = a corrupt connectivity entry, bit 1 = a wait ran out. */
+int bb_device_status(bb_ctx* ctx, void* stream, int* out);
+
+/* out[c][r] = in[r][c] for a BF16 [rows x cols] matrix. */
+int bb_transpose_bf16(bb_ctx* ctx, int64_t rows, int cols, const void* in, void* out,
+                      void* stream);
+
+/* MLP nin -> h1 -> h2 -> nout with GELU after the hidden layers (all widths multiples of 8),
+ * BF16 weights and activations, FP32 accumulation, FP32 master parameters and Adam state.
+ * Parameters are one flat FP32 vector: W1[h1][nin], b1[h1], W2[h2][h1], b2[h2],
+ * W3[nout][h2], b3[nout]; weights start uniform in +-1/sqrt(fan_in) from `seed`, biases 0. */
+typedef struct bb_mlp bb_mlp;
+int bb_mlp_create(bb_ctx* ctx, int nin, int h1, int h2, int nout, int64_t max_batch,
+                  uint64_t seed, bb_mlp** out);
+int bb_mlp_destroy(bb_mlp* m);
+int64_t bb_mlp_num_params(const bb_mlp* m);
+int bb_mlp_set_params(bb_mlp* m, const float* host, void* stream);  /* resets Adam state */
+int bb_mlp_get_params(bb_mlp* m, float* host, void* stream);
+int bb_mlp_get_grads(bb_mlp* m, float* host, void* stream);
+/* Y[B][nout] (FP32) = MLP(X[B][nin] BF16). train != 0 keeps the activations for bb_mlp_bwd
+ * and needs XT = X^T ([nin][B] BF16, kept by the caller until bb_mlp_bwd) and B % 8 == 0. */
+int bb_mlp_fwd(bb_mlp* m, int64_t B, const void* X, const void* XT, float* Y, int train,
+               void* stream);
+/* Gradients of L = 1/(B nout) sum (Y - T)^2 for the last training bb_mlp_fwd; writes L to
+ * loss_dev (one device double). */
+int bb_mlp_bwd(bb_mlp* m, int64_t B, const float* Y, const float* T, double* loss_dev,
+               void* stream);
+/* One Adam step (bias-corrected) with the stored gradients. */
+int bb_mlp_step(bb_mlp* m, float lr, float beta1, float beta2, float eps, void* stream);
+
+/* Closure features of every element of a degree-N, nf-field state q ([nf][K][Np], dtype):
+ * X[e] = scale * ( q[0..nf)[e][0..Np) , for faces f = 0..3: the neighbour's nf x Nfp
+ * coefficients on face f in this element's face ordering ) as BF16, nin = nf Np + 4 nf Nfp
+ * (840 for Maxwell at N = 5); XT (optional) receives X^T. conn as bb_solver_create. */
+int bb_closure_features(bb_ctx* ctx, int N, int64_t K, int nf, const int32_t* conn,
+                        int dtype, const void* q, float scale, void* X, void* XT,
+                        void* stream);
+/* q[f][e][p] += alpha * Y[e][f Np + p] (Y FP32 [K][nf Np]). */
+int bb_closure_apply(bb_ctx* ctx, int N, int64_t K, int nf, int dtype, float alpha,
+                     const float* Y, void* q, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
