@@ -178,6 +178,10 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=60)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--mesh-n", type=int, default=N_HEX,
+                    help="hexes per side (default: the 32^3 workload; smaller only for profiling)")
+    ap.add_argument("--tile", type=str, default=None,
+                    help="kind,elems_per_block,threads: skip the autotuner (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -198,13 +202,20 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    mesh = bbdg.uniform_tet_mesh(N_HEX)
+    mesh = bbdg.uniform_tet_mesh(args.mesh_n)
     solver = bbdg.DGSolver(mesh, N_DEG, "wave", dtype=torch.float32, tau=1.0)
     zero = lambda x, y, z: 0 * x  # noqa: E731
     q = solver.project([bbdg.gaussian_pulses(1), zero, zero, zero])
     res = torch.zeros_like(q)
     dt = solver.dt_cfl()
-    (kind, epb, nt), tune_table = autotune.tune(solver)
+    if args.tile:
+        kind, epb, nt = args.tile.split(",")
+        epb, nt = int(epb), int(nt)
+        solver.set_kernel(kind)
+        solver.set_tile(epb, nt)
+        tune_table = None
+    else:
+        (kind, epb, nt), tune_table = autotune.tune(solver)
     stream = torch.cuda.current_stream()
 
     solver.run(q, res, dt, args.warmup)
@@ -297,8 +308,8 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: 8 Gaussian pulses in p (seed 1, centres U[-0.8,0.8]^3, widths "
                     "U[0.1,0.3], amplitudes N(0,1)), u=v=w=0",
-            "config": {"workload": "wave N=9 K=196608 (32^3 hexes x 6 tets) FP32 LSRK45, "
-                                   "tau=1, dt=0.25h/(N+1)^2",
+            "config": {"workload": f"wave N=9 K={K} ({args.mesh_n}^3 hexes x 6 tets) FP32 "
+                                   "LSRK45, tau=1, dt=0.25h/(N+1)^2",
                        "N": N_DEG, "K": K, "Np": Np, "fields": NF,
                        "parallelism": f"replicas x{world}",
                        "tile": {"kernel": kind, "elems_per_block": epb, "threads": nt},

@@ -6,6 +6,8 @@
                                        vs FP64: per-field relative L2, energy drift, time
   python -m bbdg.configs --config 4    48 uneven wave/Maxwell problems in one persistent
                                        launch per stage (CUDA graph), autotuned tiles per N
+  python -m bbdg.configs --config 5    learned closure: degree-10 Maxwell data reduced to
+                                       degree 5, MLP trained on the GPU, held-out evaluation
 
 Each run prints one JSON object per line. All inputs are synthetic and seeded: no dataset
 is involved. Timings are CUDA events on the launching stream after warm-up; every input
@@ -180,9 +182,63 @@ def config4(steps: int = 100, dtype=torch.float32, compare_single: bool = True):
     return res
 
 
+def config5(n: int = 16, n_train: int = 16, nmacro_train: int = 40, epochs: int = 20,
+            n_eval: int = 2, nmacro_eval: int = 40, seed: int = 3, lr: float = 1e-3,
+            hidden=(512, 512), N_hi: int = 10, N_lo: int = 5, rollout_epochs: int = 0):
+    """Closure training and held-out evaluation. Training initial conditions are drawn from
+    `seed`, the held-out ones from seed + 1000; every number is measured on the GPU."""
+    from .closure import Closure, ClosureConfig
+    mesh = uniform_tet_mesh(n)
+    cl = Closure(mesh, ClosureConfig(N_hi=N_hi, N_lo=N_lo, hidden=tuple(hidden)), seed=seed)
+    rng = np.random.default_rng(seed)
+    train_seeds = [int(s) for s in rng.integers(0, 2**31 - 1, n_train)]
+    eval_seeds = [int(s) for s in np.random.default_rng(seed + 1000).integers(0, 2**31 - 1,
+                                                                              n_eval)]
+    head = {"config": 5, "K": mesh.K, "N_hi": N_hi, "N_lo": N_lo, "dt_hi": cl.dt_hi,
+            "macro": cl.macro, "lo_steps_per_macro": cl.lo_steps, "n_train": n_train,
+            "nmacro_train": nmacro_train, "t_train": nmacro_train * cl.macro, "epochs": epochs,
+            "n_eval": n_eval, "nmacro_eval": nmacro_eval, "t_eval": nmacro_eval * cl.macro,
+            "mlp": list(cl.net.dims), "params": cl.net.num_params,
+            "rollout_epochs": rollout_epochs}
+    print(json.dumps(head), flush=True)
+    cl.fit_scales(train_seeds[0], 3)
+    info = cl.train(train_seeds, nmacro_train, epochs=epochs, lr=lr, lr_final=lr / 100,
+                    rollout_epochs=rollout_epochs,
+                    log=lambda s: print(s, flush=True))
+    info.update({"s_in": cl.s_in, "s_out": cl.s_out})
+    print(json.dumps({"train": info}), flush=True)
+    rows = []
+    for s in eval_seeds:
+        r = cl.evaluate(s, nmacro_eval)
+        r.update(cl.apriori(s, nmacro_eval))
+        rows.append(r)
+        print(json.dumps(r), flush=True)
+    summ = {"config": 5, "summary": True,
+            "err_plain_lo_mean": float(np.mean([r["err_plain_lo"] for r in rows])),
+            "err_closure_lo_mean": float(np.mean([r["err_closure_lo"] for r in rows])),
+            "err_hi_vs_fp64_hi_mean": float(np.mean([r["err_hi_vs_fp64_hi"] for r in rows])),
+            "closure_gain_mean": float(np.mean([r["closure_gain"] for r in rows])),
+            "apriori_gain_mean": float(np.mean([r["apriori_gain"] for r in rows])),
+            "speedup_closure_vs_hi_mean": float(np.mean([r["speedup_closure_vs_hi"]
+                                                         for r in rows]))}
+    print(json.dumps(summ), flush=True)
+    return cl, info, rows, summ
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--config", type=int, required=True, choices=[2, 3, 4])
+    ap.add_argument("--config", type=int, required=True, choices=[2, 3, 4, 5])
+    ap.add_argument("--n", type=int, default=16)
+    ap.add_argument("--n-train", type=int, default=16)
+    ap.add_argument("--nmacro-train", type=int, default=40)
+    ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--n-eval", type=int, default=2)
+    ap.add_argument("--nmacro-eval", type=int, default=40)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--hidden", type=str, default="512,512")
+    ap.add_argument("--N-hi", type=int, default=10)
+    ap.add_argument("--N-lo", type=int, default=5)
+    ap.add_argument("--rollout-epochs", type=int, default=0)
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--degrees", type=str, default="3-15")
     a = ap.parse_args()
@@ -191,8 +247,13 @@ def main():
         config2(range(lo, hi + 1))
     elif a.config == 3:
         config3(steps=a.steps or 200)
-    else:
+    elif a.config == 4:
         config4(steps=a.steps or 100)
+    else:
+        config5(n=a.n, n_train=a.n_train, nmacro_train=a.nmacro_train, epochs=a.epochs,
+                n_eval=a.n_eval, nmacro_eval=a.nmacro_eval, lr=a.lr,
+                hidden=tuple(int(v) for v in a.hidden.split(",")), N_hi=a.N_hi, N_lo=a.N_lo,
+                rollout_epochs=a.rollout_epochs)
 
 
 if __name__ == "__main__":

