@@ -77,7 +77,7 @@ SIGNATURES.update({
     "bb_batch_get_tile": (_I, [_P, _I, _I, ctypes.POINTER(_I)]),
     "bb_batch_run": (_I, [_P, _I, _I, _P]),
     "bb_gemm_bf16": (_I, [_P, _I64, _I, _I, _P, _P, ctypes.c_float, _P, _I, _P, _P, _P, _P, _P,
-                          _I, _I, _P]),
+                          _I, _I, _I, _P]),
     "bb_device_status": (_I, [_P, _P, ctypes.POINTER(_I)]),
     "bb_transpose_bf16": (_I, [_P, _I64, _I, _P, _P, _P]),
     "bb_mlp_create": (_I, [_P, _I, _I, _I, _I, _I64, ctypes.c_uint64, ctypes.POINTER(_P)]),

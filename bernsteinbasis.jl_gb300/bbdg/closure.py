@@ -135,20 +135,28 @@ class Closure:
                 self.correct(q)
 
     # ---- data ----------------------------------------------------------------------------
-    def snapshots(self, seed: int, nmacro: int, rollout: bool = False):
+    def snapshots(self, seed: int, nmacro: int, rollout: bool = False, noise: float = 0.0):
         """Yields (features BF16 [K, nin], target FP32 [K, nout]) for nmacro macro steps of
         one initial condition, scaled by the current s_in and s_out.
 
         rollout=False: every input starts from the reduced degree-N_hi state (teacher forced).
         rollout=True: inputs follow the closure-corrected degree-N_lo trajectory of the
-        current network, so the targets also carry the error it has accumulated."""
+        current network, so the targets also carry the error it has accumulated.
+        noise > 0: the teacher-forced input state is perturbed by Gaussian noise of that
+        relative size (per field RMS) before the plain macro step, and the target still
+        points at the reduced degree-N_hi state, so the network also learns to remove
+        perturbations like the ones a corrected run accumulates."""
         hi = self.hi_solver()
         q = self.initial_state(seed)
         res = torch.zeros_like(q)
         c = project(q, self.cfg.N_hi, self.cfg.N_lo)
         traj = c.clone()
+        gen = torch.Generator(device=self.device).manual_seed(seed ^ 0x5DEECE66D)
         for _ in range(nmacro):
             s = (traj if rollout else c).clone()
+            if noise > 0 and not rollout:
+                rms = s.pow(2).mean(dim=(1, 2), keepdim=True).sqrt()
+                s += noise * rms * torch.randn(s.shape, generator=gen, device=self.device)
             self.plain_macro(s)
             hi.run(q, res, self.dt_hi, self.cfg.hi_steps)
             c = project(q, self.cfg.N_hi, self.cfg.N_lo, out=c)
@@ -172,7 +180,7 @@ class Closure:
         self.s_out = 1.0 / math.sqrt(max(ft / n, 1e-30))
 
     def train(self, seeds, nmacro: int, epochs: int = 20, lr: float = 1e-3,
-              lr_final: float = 1e-5, rollout_epochs: int = 0,
+              lr_final: float = 1e-5, rollout_epochs: int = 0, noise: float = 0.0,
               store_limit_bytes: float = 40e9, log=None) -> dict:
         """Teacher-forced phase: generates the snapshot pairs of every seed (kept on the GPU
         up to the store limit) and runs `epochs` passes of Adam over them in shuffled order,
@@ -182,7 +190,7 @@ class Closure:
         t0 = time.perf_counter()
         per = self.K * (self.nin * 2 + self.nout * 4)
         cap = max(1, int(store_limit_bytes // per))
-        store = self._generate(seeds, nmacro, False, cap)
+        store = self._generate(seeds, nmacro, False, cap, noise)
         torch.cuda.synchronize()
         info = {"snapshots": len(store), "generate_s": time.perf_counter() - t0}
         losses = self._fit(store, epochs, lr, lr_final, log)
@@ -197,10 +205,10 @@ class Closure:
                          "rollout_epoch_loss": losses2})
         return info
 
-    def _generate(self, seeds, nmacro, rollout, cap):
+    def _generate(self, seeds, nmacro, rollout, cap, noise=0.0):
         store = []
         for s in seeds:
-            for X, T in self.snapshots(s, nmacro, rollout):
+            for X, T in self.snapshots(s, nmacro, rollout, noise):
                 if len(store) < cap:
                     store.append((X, T))
         return store

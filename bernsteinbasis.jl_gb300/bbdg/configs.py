@@ -184,7 +184,8 @@ def config4(steps: int = 100, dtype=torch.float32, compare_single: bool = True):
 
 def config5(n: int = 16, n_train: int = 16, nmacro_train: int = 40, epochs: int = 20,
             n_eval: int = 2, nmacro_eval: int = 40, seed: int = 3, lr: float = 1e-3,
-            hidden=(512, 512), N_hi: int = 10, N_lo: int = 5, rollout_epochs: int = 0):
+            hidden=(512, 512), N_hi: int = 10, N_lo: int = 5, rollout_epochs: int = 0,
+            noise: float = 0.0):
     """Closure training and held-out evaluation. Training initial conditions are drawn from
     `seed`, the held-out ones from seed + 1000; every number is measured on the GPU."""
     from .closure import Closure, ClosureConfig
@@ -199,11 +200,11 @@ def config5(n: int = 16, n_train: int = 16, nmacro_train: int = 40, epochs: int 
             "nmacro_train": nmacro_train, "t_train": nmacro_train * cl.macro, "epochs": epochs,
             "n_eval": n_eval, "nmacro_eval": nmacro_eval, "t_eval": nmacro_eval * cl.macro,
             "mlp": list(cl.net.dims), "params": cl.net.num_params,
-            "rollout_epochs": rollout_epochs}
+            "rollout_epochs": rollout_epochs, "noise": noise}
     print(json.dumps(head), flush=True)
     cl.fit_scales(train_seeds[0], 3)
     info = cl.train(train_seeds, nmacro_train, epochs=epochs, lr=lr, lr_final=lr / 100,
-                    rollout_epochs=rollout_epochs,
+                    rollout_epochs=rollout_epochs, noise=noise,
                     log=lambda s: print(s, flush=True))
     info.update({"s_in": cl.s_in, "s_out": cl.s_out})
     print(json.dumps({"train": info}), flush=True)
@@ -239,6 +240,7 @@ def main():
     ap.add_argument("--N-hi", type=int, default=10)
     ap.add_argument("--N-lo", type=int, default=5)
     ap.add_argument("--rollout-epochs", type=int, default=0)
+    ap.add_argument("--noise", type=float, default=0.0)
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--degrees", type=str, default="3-15")
     a = ap.parse_args()
@@ -253,7 +255,7 @@ def main():
         config5(n=a.n, n_train=a.n_train, nmacro_train=a.nmacro_train, epochs=a.epochs,
                 n_eval=a.n_eval, nmacro_eval=a.nmacro_eval, lr=a.lr,
                 hidden=tuple(int(v) for v in a.hidden.split(",")), N_hi=a.N_hi, N_lo=a.N_lo,
-                rollout_epochs=a.rollout_epochs)
+                rollout_epochs=a.rollout_epochs, noise=a.noise)
 
 
 if __name__ == "__main__":

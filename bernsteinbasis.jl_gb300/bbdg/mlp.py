@@ -20,11 +20,14 @@ def _ctx_of(t: torch.Tensor):
 
 
 def gemm_bf16(A: torch.Tensor, B: torch.Tensor, *, alpha: float = 1.0, bias=None, act: int = 0,
-              pre=None, out_f32=None, out_bf16=None, out_t=None, bias_grad=None, stream=None):
+              pre=None, out_f32=None, out_bf16=None, out_t=None, bias_grad=None, kt_per: int = 0,
+              stream=None):
     """C = alpha A B^T (A [M, K], B [N, K], BF16) with the fused epilogue of bb_gemm_bf16.
 
     Outputs are caller tensors (out_f32 [M, N] float32, out_bf16 [M, N] bfloat16, out_t [N, M]
-    bfloat16, bias_grad [N] float32, pre [M, N] float32); returns out_f32."""
+    bfloat16, bias_grad [N] float32, pre [M, N] float32); returns out_f32. kt_per > 0 splits
+    K into chunks of kt_per x 64 whose partial products are added into out_f32 (zero it first;
+    no other output allowed)."""
     require_cuda(A, B)
     if A.dtype != torch.bfloat16 or B.dtype != torch.bfloat16:
         raise TypeError("operands must be bfloat16")
@@ -40,7 +43,7 @@ def gemm_bf16(A: torch.Tensor, B: torch.Tensor, *, alpha: float = 1.0, bias=None
     ctx = _ctx_of(A)
     ctx.check(_lib.load().bb_gemm_bf16(
         ctx.handle, M, N, K, ptr(A), ptr(B), float(alpha), ptr(bias), int(act), ptr(pre),
-        ptr(out_f32), ptr(out_bf16), ptr(out_t), ptr(bias_grad), ldc, ldt,
+        ptr(out_f32), ptr(out_bf16), ptr(out_t), ptr(bias_grad), ldc, ldt, int(kt_per),
         stream_handle(stream)), "bb_gemm_bf16")
     return out_f32
 

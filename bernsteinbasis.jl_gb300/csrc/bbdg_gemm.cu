@@ -1,12 +1,23 @@
 // BF16 tensor-core GEMM for sm_103a (tcgen05 + TMEM + TMA), FP32 accumulation:
-//     C[M x N] = alpha * A[M x K] * B[N x K]^T (+ bias[N]) (optionally GELU)
-// A and B are row-major BF16 with K contiguous ("K-major" operands). One CTA computes one
-// 128 x 128 tile: TMA loads 128 x 64 boxes of A and B with 128-byte swizzle into a 4-stage
-// shared-memory ring (mbarrier full/empty pairs, every wait bounded); one thread issues
-// tcgen05.mma (kind::f16, M=128, N=128, K=16) into a TMEM accumulator and releases each
-// stage with tcgen05.commit; after the last K block the four warps read the accumulator with
-// tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = tile rows) and apply the epilogue.
-// Used by the learned per-element closure (an MLP trained and evaluated in BF16).
+//     C[M x N] = alpha * A[M x K] * B[N x K]^T, then a fused epilogue (bbdg_gemm.cuh).
+// A and B are row-major BF16 with K contiguous ("K-major" operands).
+//
+// Persistent, warp-specialised kernel, one CTA per SM (192 threads):
+//   warp 0      TMA producer: 128 x 64 boxes of A and BN x 64 boxes of B, 128-byte swizzle,
+//               into a STAGES-deep shared-memory ring (mbarrier full / empty pairs);
+//   warp 1      MMA issuer: one thread issues tcgen05.mma (kind::f16, M=128, N=BN, K=16)
+//               into one of two TMEM accumulators and releases ring stages and finished
+//               accumulators with tcgen05.commit;
+//   warps 2-5   epilogue: tcgen05.ld of 32-column chunks (warp w reads TMEM lanes
+//               32(w%4)..+31 = tile rows), staged through a per-warp shared tile so that
+//               every global store of a warp covers one contiguous row segment (row-major
+//               outputs) or one contiguous column segment (the transposed output).
+// The two accumulators let the epilogue of tile i overlap the main loop of tile i+1.
+// Tiles are visited n-fastest so that CTAs running together share A rows in L2; split-K
+// partial tiles (gridless: part of the tile index) add into the FP32 output atomically.
+// Every mbarrier wait is bounded (about a second): on time-out the kernel sets the status
+// word, stops issuing work, lets its copies and MMAs in flight finish (bounded) and frees
+// its TMEM. Used by the learned per-element closure (an MLP trained and run in BF16).
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -18,19 +29,6 @@
 #include "bbdg_gemm.cuh"
 
 namespace {
-
-constexpr int BM = 128, BN = 128, BK = 64, STAGES = 4, UMMA_K = 16;
-constexpr int A_BYTES = BM * BK * 2;  // 16 KiB per stage
-constexpr int B_BYTES = BN * BK * 2;  // 16 KiB per stage
-constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int TMEM_COLS = BN;         // 128 FP32 accumulator columns
-constexpr int GEMM_THREADS = 128;
-constexpr int GEMM_SMEM = STAGES * STAGE_BYTES + 1024 /*alignment slack*/ + 256 /*barriers*/;
-
-// tcgen05 instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16 (bits 7-9,
-// 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                            ((uint32_t)(BM >> 4) << 24);
 
 __device__ __forceinline__ uint32_t saddr(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -92,6 +90,9 @@ __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t 
       "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
       : "memory");
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(b)) : "memory");
+}
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                    saddr(bar))
@@ -103,17 +104,23 @@ __device__ __forceinline__ void tc_fence_before() {
 __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
-// 32 lanes x 32 bit, 16 consecutive columns per thread.
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+// 32 lanes x 32 bit, 32 consecutive columns per thread (warp w % 4 reads lanes 32(w%4)..+31).
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
-      "%11, %12, %13, %14, %15}, [%16];"
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
+      "%28, %29, %30, %31}, [%32];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
         "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15])
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr)
       : "memory");
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
 }
 
 __device__ __forceinline__ float gelu(float x) {
@@ -125,38 +132,75 @@ __device__ __forceinline__ float gelu_grad(float x) {
          x * 0.39894228040143268f * expf(-0.5f * x * x);
 }
 
-constexpr int EPI_PITCH = BN + 1;  // staged FP32 tile pitch (conflict-free rows and columns)
-static_assert(BM * EPI_PITCH * 4 <= STAGES * STAGE_BYTES, "epilogue tile must fit the ring");
+template <int BN_>
+struct GemmCfg {
+  static constexpr int BM = 128, BN = BN_, BK = 64, UMMA_K = 16;
+  static constexpr int A_BYTES = BM * BK * 2;            // 16 KiB
+  static constexpr int B_BYTES = BN * BK * 2;            // 32 or 16 KiB
+  static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+  static constexpr int STAGES = (192 * 1024) / STAGE_BYTES;  // 4 or 6
+  static constexpr int TMEM_COLS = 2 * BN;               // two FP32 accumulators
+  static constexpr int EPI_WARPS = 4;
+  static constexpr int THREADS = 64 + 32 * EPI_WARPS;
+  static constexpr int EPI_PITCH = 33;                   // floats; conflict-free both ways
+  static constexpr int EPI_BYTES = EPI_WARPS * 32 * EPI_PITCH * 4;
+  static constexpr int NBAR = 2 * STAGES + 5;
+  static constexpr int SMEM = STAGES * STAGE_BYTES + EPI_BYTES + 8 * NBAR + 16 + 1024;
+  // instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16 (bits 7-9 and
+  // 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+  static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) |
+                                    ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+  static_assert(SMEM <= 227 * 1024, "shared memory budget");
+  static_assert(TMEM_COLS <= 512, "TMEM budget");
+};
 
-__global__ void __launch_bounds__(GEMM_THREADS) gemm_bf16_tn_kernel(
-    const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-    GemmEpilogue ep) {
+struct TileSched {
+  int m_tiles, n_tiles, splits, kt_per, nkt_all;
+  __device__ __forceinline__ void decode(int tile, int& mt, int& nt, int& kt0, int& nkt) const {
+    nt = tile % n_tiles;
+    const int rest = tile / n_tiles;
+    mt = rest % m_tiles;
+    const int z = rest / m_tiles;
+    kt0 = z * kt_per;
+    nkt = min(kt_per, nkt_all - kt0);
+  }
+  __host__ __device__ __forceinline__ int total() const { return m_tiles * n_tiles * splits; }
+};
+
+__device__ __forceinline__ bool flag_set(const volatile int* f) { return *f != 0; }
+
+template <int BN>
+__global__ void __launch_bounds__(GemmCfg<BN>::THREADS, 1)
+    gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tmA,
+                        const __grid_constant__ CUtensorMap tmB, GemmEpilogue ep, TileSched ts) {
+  using C = GemmCfg<BN>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  // 1024-byte aligned stage ring (required by the 128-byte swizzle atoms)
   const uint32_t base = saddr(smem_raw);
-  unsigned char* smem = smem_raw + ((1024 - (base & 1023)) & 1023);
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
-  uint64_t* empty = full + STAGES;
-  uint64_t* accum = empty + STAGES;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
-  __shared__ int s_fail, s_issued, s_consumed;
+  unsigned char* smem = smem_raw + ((1024 - (base & 1023)) & 1023);  // 1024-aligned ring
+  float* epi = reinterpret_cast<float*>(smem + C::STAGES * C::STAGE_BYTES);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::STAGES * C::STAGE_BYTES + C::EPI_BYTES);
+  uint64_t* full = bars;                    // [STAGES] TMA -> MMA
+  uint64_t* empty = bars + C::STAGES;       // [STAGES] MMA -> TMA
+  uint64_t* tfull = bars + 2 * C::STAGES;   // [2] MMA -> epilogue
+  uint64_t* tempty = tfull + 2;             // [2] epilogue -> MMA
+  uint64_t* mdone = tempty + 2;             // every MMA of this CTA complete
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + C::NBAR);
+  __shared__ int s_abort, s_issued, s_consumed;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-  // K blocks [kt0, kt0 + nkt) of this CTA (split-K along gridDim.z)
-  const int nkt_all = (ep.K + BK - 1) / BK;
-  const int kt0 = blockIdx.z * ep.kt_per;
-  const int nkt = min(ep.kt_per, nkt_all - kt0);
-
   if (threadIdx.x == 0) {
-    s_fail = 0;
+    s_abort = 0;
     s_issued = 0;
     s_consumed = 0;
-    for (int s = 0; s < STAGES; ++s) {
+    for (int s = 0; s < C::STAGES; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(accum, 1);
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(&tfull[a], 1);
+      mbar_init(&tempty[a], C::EPI_WARPS);
+    }
+    mbar_init(mdone, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -164,7 +208,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) gemm_bf16_tn_kernel(
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      saddr(tmem_slot)),
-                 "r"(TMEM_COLS)
+                 "r"(C::TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -172,110 +216,155 @@ __global__ void __launch_bounds__(GEMM_THREADS) gemm_bf16_tn_kernel(
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  volatile int* abort_flag = &s_abort;
+  const int total = ts.total();
 
-  if (warp == 0 && lane == 0) {
-    // TMA producer
-    int kt = 0;
-    for (; kt < nkt; ++kt) {
-      const int s = kt % STAGES;
-      const uint32_t ph = (kt / STAGES) & 1;
-      if (!mbar_wait(&empty[s], ph ^ 1)) {
-        atomicOr(ep.status, 2);
-        s_fail = 1;
-        break;
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- TMA producer ----
+      int it = 0;
+      for (int tile = blockIdx.x; tile < total && !flag_set(abort_flag); tile += gridDim.x) {
+        int mt, nt, kt0, nkt;
+        ts.decode(tile, mt, nt, kt0, nkt);
+        for (int kt = 0; kt < nkt; ++kt, ++it) {
+          const int s = it % C::STAGES;
+          if (!mbar_wait(&empty[s], ((it / C::STAGES) & 1) ^ 1)) {
+            atomicOr(ep.status, 2);
+            *abort_flag = 1;
+            break;
+          }
+          unsigned char* st = smem + s * C::STAGE_BYTES;
+          mbar_expect_tx(&full[s], C::STAGE_BYTES);
+          tma_load_2d(st, &tmA, (kt0 + kt) * C::BK, mt * C::BM, &full[s]);
+          tma_load_2d(st + C::A_BYTES, &tmB, (kt0 + kt) * C::BK, nt * BN, &full[s]);
+        }
       }
-      unsigned char* st = smem + s * STAGE_BYTES;
-      mbar_expect_tx(&full[s], STAGE_BYTES);
-      tma_load_2d(st, &tmA, (kt0 + kt) * BK, m0, &full[s]);
-      tma_load_2d(st + A_BYTES, &tmB, (kt0 + kt) * BK, n0, &full[s]);
+      s_issued = it;
     }
-    s_issued = kt;
-  } else if (warp == 1 && lane == 0) {
-    // MMA issuer
-    int kt = 0;
-    for (; kt < nkt; ++kt) {
-      const int s = kt % STAGES;
-      const uint32_t ph = (kt / STAGES) & 1;
-      if (!mbar_wait(&full[s], ph)) {
-        atomicOr(ep.status, 2);
-        s_fail = 1;
-        break;
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer ----
+      int it = 0, local = 0;
+      for (int tile = blockIdx.x; tile < total && !flag_set(abort_flag);
+           tile += gridDim.x, ++local) {
+        int mt, nt, kt0, nkt;
+        ts.decode(tile, mt, nt, kt0, nkt);
+        const int a = local & 1;
+        if (!mbar_wait(&tempty[a], ((local >> 1) & 1) ^ 1)) {
+          atomicOr(ep.status, 2);
+          *abort_flag = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t d = tmem + (uint32_t)(a * BN);
+        bool ok = true;
+        for (int kt = 0; kt < nkt; ++kt, ++it) {
+          const int s = it % C::STAGES;
+          if (!mbar_wait(&full[s], (it / C::STAGES) & 1)) {
+            atomicOr(ep.status, 2);
+            *abort_flag = 1;
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a0 = saddr(smem + s * C::STAGE_BYTES);
+          const uint32_t b0 = a0 + C::A_BYTES;
+#pragma unroll
+          for (int k = 0; k < C::BK / C::UMMA_K; ++k)  // 16 BF16 = 32 bytes along K per MMA
+            umma_bf16(d, sw128_desc(a0 + k * 32), sw128_desc(b0 + k * 32), C::IDESC,
+                      (kt | k) != 0);
+          umma_commit(&empty[s]);
+        }
+        if (!ok) break;
+        umma_commit(&tfull[a]);
       }
+      s_consumed = it;
+      umma_commit(mdone);
+    }
+  } else {
+    // ---- epilogue warps ----
+    const int g = warp & 3;  // TMEM lane quarter this warp may access
+    float* T = epi + (warp - 2) * 32 * C::EPI_PITCH;
+    int local = 0;
+    for (int tile = blockIdx.x; tile < total; tile += gridDim.x, ++local) {
+      int mt, nt, kt0, nkt;
+      ts.decode(tile, mt, nt, kt0, nkt);
+      const int a = local & 1;
+      int ok = 0;
+      if (lane == 0) {
+        ok = !flag_set(abort_flag) && mbar_wait(&tfull[a], (local >> 1) & 1);
+        if (!ok && !flag_set(abort_flag)) {
+          atomicOr(ep.status, 2);
+          *abort_flag = 1;
+        }
+      }
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) break;
       tc_fence_after();
-      const uint32_t a0 = saddr(smem + s * STAGE_BYTES);
-      const uint32_t b0 = a0 + A_BYTES;
-#pragma unroll
-      for (int k = 0; k < BK / UMMA_K; ++k) {
-        // advance 16 BF16 = 32 bytes along K inside the 128-byte swizzle row
-        umma_bf16(tmem, sw128_desc(a0 + k * 32), sw128_desc(b0 + k * 32), kIdesc,
-                  (kt | k) != 0);
-      }
-      umma_commit(&empty[s]);  // frees the stage when these MMAs have read it
-    }
-    s_consumed = kt;
-    umma_commit(accum);        // accumulator complete (tracks every MMA issued above)
-  }
-  __syncthreads();
-  // one thread observes the accumulator barrier; the block learns the outcome uniformly
-  // (the TMEM loads below are warp-collective)
-  __shared__ int s_ok;
-  if (threadIdx.x == 0) {
-    s_ok = mbar_wait(accum, 0) ? 1 : 0;
-    if (!s_ok) atomicOr(ep.status, 2);
-  }
-  __syncthreads();
-  tc_fence_after();
-  const bool ok = s_ok != 0;
-  if (s_fail) {
-    // a wait ran out: let the loads still in flight land before the CTA exits
-    if (threadIdx.x == 0)
-      for (int kt = s_consumed; kt < s_issued; ++kt) mbar_wait(&full[kt % STAGES], (kt / STAGES) & 1);
-  } else if (ok && nkt > 0) {
-    // 1) TMEM -> shared FP32 tile (warp w holds TMEM lanes = tile rows 32w..32w+31)
-    float* S = reinterpret_cast<float*>(smem);
-    const int r = warp * 32 + lane;
+      const int r0 = mt * C::BM + g * 32;
+      const int n0 = nt * BN;
 #pragma unroll 1
-    for (int c0 = 0; c0 < BN; c0 += 16) {
-      uint32_t v[16];
-      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        float v[32];
+        tmem_ld32(tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(a * BN + c0), v);
+        if (c0 + 32 == BN) {
+          // accumulator fully read: hand it back to the MMA warp
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&tempty[a]);
+        }
+        if (n0 + c0 >= ep.N) continue;
 #pragma unroll
-      for (int j = 0; j < 16; ++j) S[r * EPI_PITCH + c0 + j] = __uint_as_float(v[j]);
-    }
-    __syncthreads();
-    // 2) row pass: thread t owns column t, coalesced row-major reads and writes
-    const int c = n0 + threadIdx.x;
-    const int rows = min(BM, ep.M - m0);
-    if (c < ep.N) {
-      const float b = ep.bias ? ep.bias[c] : 0.0f;
-      float gsum = 0.0f;
-      for (int rr = 0; rr < rows; ++rr) {
-        const size_t off = (size_t)(m0 + rr) * ep.ldc + c;
-        float v = fmaf(ep.alpha, S[rr * EPI_PITCH + threadIdx.x], b);
-        if (ep.act == 1) {
-          if (ep.Pre) ep.Pre[off] = v;
-          v = gelu(v);
-        } else if (ep.act == 2) {
-          v *= gelu_grad(ep.Pre[off]);
+        for (int j = 0; j < 32; ++j) T[lane * C::EPI_PITCH + j] = v[j];
+        __syncwarp();
+        // row pass: lane owns column c; each store covers one contiguous row segment
+        const int c = n0 + c0 + lane;
+        const bool cin = c < ep.N;
+        const float b = (cin && ep.bias) ? ep.bias[c] : 0.0f;
+        float gsum = 0.0f;
+        const int rows = min(32, ep.M - r0);
+        for (int rr = 0; rr < rows; ++rr) {
+          float x = fmaf(ep.alpha, T[rr * C::EPI_PITCH + lane], b);
+          if (cin) {
+            const size_t off = (size_t)(r0 + rr) * ep.ldc + c;
+            if (ep.act == 1) {
+              if (ep.Pre) ep.Pre[off] = x;
+              x = gelu(x);
+            } else if (ep.act == 2) {
+              x *= gelu_grad(ep.Pre[off]);
+            }
+            if (ep.Cf) {
+              if (ep.kt_per < ts.nkt_all) atomicAdd(ep.Cf + off, x);
+              else ep.Cf[off] = ep.accumulate ? ep.Cf[off] + x : x;
+            }
+            if (ep.Cb) ep.Cb[off] = __float2bfloat16_rn(x);
+            gsum += x;
+          }
+          T[rr * C::EPI_PITCH + lane] = x;
         }
-        if (ep.Cf) {
-          if (gridDim.z > 1) atomicAdd(ep.Cf + off, v);
-          else ep.Cf[off] = ep.accumulate ? ep.Cf[off] + v : v;
+        if (ep.bias_grad && cin) atomicAdd(ep.bias_grad + c, gsum);
+        if (ep.CbT) {
+          // column pass: lane owns row r0 + lane; each store covers one column segment
+          __syncwarp();
+          if (lane < rows) {
+            const int cols = min(32, ep.N - (n0 + c0));
+            __nv_bfloat16* o = ep.CbT + (size_t)(n0 + c0) * ep.ldt + r0 + lane;
+            for (int j = 0; j < cols; ++j)
+              o[(size_t)j * ep.ldt] = __float2bfloat16_rn(T[lane * C::EPI_PITCH + j]);
+          }
         }
-        if (ep.Cb) ep.Cb[off] = __float2bfloat16_rn(v);
-        gsum += v;
-        S[rr * EPI_PITCH + threadIdx.x] = v;
+        __syncwarp();
       }
-      if (ep.bias_grad) atomicAdd(ep.bias_grad + c, gsum);
     }
-    // 3) column pass for the transposed BF16 output: thread t owns row t
-    if (ep.CbT) {
-      __syncthreads();
-      if (threadIdx.x < rows) {
-        const int cols = min(BN, ep.N - n0);
-        __nv_bfloat16* o = ep.CbT + (size_t)n0 * ep.ldt + m0 + threadIdx.x;
-        for (int cc = 0; cc < cols; ++cc)
-          o[(size_t)cc * ep.ldt] = __float2bfloat16_rn(S[threadIdx.x * EPI_PITCH + cc]);
-      }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // MMAs still in flight (normal exit: none) must finish before TMEM is freed
+    if (!mbar_wait(mdone, 0)) atomicOr(ep.status, 2);
+    if (flag_set(abort_flag)) {
+      // copies issued but never consumed land before the CTA exits
+      for (int it = s_consumed; it < s_issued; ++it)
+        mbar_wait(&full[it % C::STAGES], (it / C::STAGES) & 1);
     }
   }
   tc_fence_before();
@@ -283,7 +372,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) gemm_bf16_tn_kernel(
   if (warp == 0) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                 "r"(TMEM_COLS)
+                 "r"(C::TMEM_COLS)
                  : "memory");
   }
 }
@@ -306,7 +395,7 @@ int get_encoder(bb_ctx* ctx) {
 int make_map(bb_ctx* ctx, CUtensorMap* tm, const void* ptr, int64_t rows, int K, int box_rows) {
   cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)K * 2};
-  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t box[2] = {64u, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = g_encode(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims,
                         strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -316,25 +405,47 @@ int make_map(bb_ctx* ctx, CUtensorMap* tm, const void* ptr, int64_t rows, int K,
   return BB_OK;
 }
 
+template <int BN>
+int launch_bn(bb_ctx* ctx, const CUtensorMap& ta, const void* B, int N, int K, GemmEpilogue ep,
+              TileSched ts, cudaStream_t st) {
+  using C = GemmCfg<BN>;
+  CUtensorMap tb;
+  int rc = make_map(ctx, &tb, B, N, K, BN);
+  if (rc) return rc;
+  static std::mutex attr_mu;
+  static uint64_t attr_done = 0;  // one bit per device
+  {
+    std::lock_guard<std::mutex> lock(attr_mu);
+    const uint64_t bit = 1ull << (ctx->device & 63);
+    if (!(attr_done & bit)) {
+      BB_CUDA(ctx, cudaFuncSetAttribute(gemm_bf16_tn_kernel<BN>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+      attr_done |= bit;
+    }
+  }
+  const int grid = std::min(ts.total(), ctx->num_sms);
+  gemm_bf16_tn_kernel<BN><<<grid, C::THREADS, C::SMEM, st>>>(ta, tb, ep, ts);
+  return bb_check_launch(ctx, "gemm_bf16_tn_kernel");
+}
+
 }  // namespace
 
 int bb_gemm_launch(bb_ctx* ctx, int64_t M, int N, int K, const void* A, const void* B,
                    GemmEpilogue ep, cudaStream_t st) {
   if (M < 1 || N < 1 || K < 1) return bb_fail(ctx, BB_ERR_ARG, "GEMM sizes must be positive");
   if (K % 8 != 0) return bb_fail(ctx, BB_ERR_ARG, "GEMM K must be a multiple of 8 (16-byte rows)");
-  if (((uintptr_t)A | (uintptr_t)B) & 15) return bb_fail(ctx, BB_ERR_ARG, "GEMM operands must be 16-byte aligned");
-  if (M > (int64_t)65535 * BM) return bb_fail(ctx, BB_ERR_ARG, "GEMM M too large");
+  if (((uintptr_t)A | (uintptr_t)B) & 15)
+    return bb_fail(ctx, BB_ERR_ARG, "GEMM operands must be 16-byte aligned");
+  if (M > ((int64_t)1 << 30) / 2) return bb_fail(ctx, BB_ERR_ARG, "GEMM M too large");
   int rc = get_encoder(ctx);
   if (rc) return rc;
-  CUtensorMap ta, tb;
-  rc = make_map(ctx, &ta, A, M, K, BM);
-  if (rc) return rc;
-  rc = make_map(ctx, &tb, B, N, K, BN);
+  CUtensorMap ta;
+  rc = make_map(ctx, &ta, A, M, K, 128);
   if (rc) return rc;
   ep.M = (int)M;
   ep.N = N;
   ep.K = K;
-  const int nkt = (K + BK - 1) / BK;
+  const int nkt = (K + 63) / 64;
   int splits = 1;
   if (ep.kt_per > 0 && ep.kt_per < nkt) {
     // split-K: partial products are added into Cf (which the caller has zeroed)
@@ -344,20 +455,19 @@ int bb_gemm_launch(bb_ctx* ctx, int64_t M, int N, int K, const void* A, const vo
   } else {
     ep.kt_per = nkt;
   }
-  static std::mutex attr_mu;
-  static uint64_t attr_done = 0;  // one bit per device
-  {
-    std::lock_guard<std::mutex> lock(attr_mu);
-    const uint64_t bit = 1ull << (ctx->device & 63);
-    if (!(attr_done & bit)) {
-      BB_CUDA(ctx, cudaFuncSetAttribute(gemm_bf16_tn_kernel,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, GEMM_SMEM));
-      attr_done |= bit;
-    }
-  }
-  dim3 grid((N + BN - 1) / BN, (unsigned)((M + BM - 1) / BM), splits);
-  gemm_bf16_tn_kernel<<<grid, GEMM_THREADS, GEMM_SMEM, st>>>(ta, tb, ep);
-  return bb_check_launch(ctx, "gemm_bf16_tn_kernel");
+  // BN = 256 unless 128-column tiles waste less of the last tile
+  const int pad256 = (N + 255) / 256 * 256 - N, pad128 = (N + 127) / 128 * 128 - N;
+  const int bn = pad256 <= pad128 ? 256 : 128;
+  TileSched ts;
+  ts.m_tiles = (int)((M + 127) / 128);
+  ts.n_tiles = (N + bn - 1) / bn;
+  ts.splits = splits;
+  ts.kt_per = ep.kt_per;
+  ts.nkt_all = nkt;
+  if ((int64_t)ts.m_tiles * ts.n_tiles * splits > INT32_MAX / 2)
+    return bb_fail(ctx, BB_ERR_ARG, "GEMM too large");
+  return bn == 256 ? launch_bn<256>(ctx, ta, B, N, K, ep, ts, st)
+                   : launch_bn<128>(ctx, ta, B, N, K, ep, ts, st);
 }
 
 int* bb_ctx_status_word(bb_ctx* ctx) {
@@ -371,7 +481,7 @@ int* bb_ctx_status_word(bb_ctx* ctx) {
 extern "C" int bb_gemm_bf16(bb_ctx* ctx, int64_t M, int N, int K, const void* A, const void* B,
                             float alpha, const float* bias, int act, float* pre, float* C_f32,
                             void* C_bf16, void* CT_bf16, float* bias_grad, int ldc, int ldt,
-                            void* stream) {
+                            int kt_per, void* stream) {
   if (!ctx) return BB_ERR_ARG;
   if (!A || !B || (!C_f32 && !C_bf16 && !CT_bf16 && !bias_grad))
     return bb_fail(ctx, BB_ERR_ARG, "bb_gemm_bf16: null operand or no output");
@@ -396,6 +506,8 @@ extern "C" int bb_gemm_bf16(bb_ctx* ctx, int64_t M, int N, int K, const void* A,
   ep.ldc = ldc;
   ep.ldt = ldt;
   ep.status = status;
+  if (kt_per < 0) return bb_fail(ctx, BB_ERR_ARG, "kt_per must be >= 0");
+  ep.kt_per = kt_per;
   return bb_gemm_launch(ctx, M, N, K, A, B, ep, (cudaStream_t)stream);
 }
 

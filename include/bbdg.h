@@ -205,11 +205,14 @@ int bb_mass_norms(bb_ctx* ctx, int N, int64_t K, int nf, int dtype, const void* 
  *   v += bias[c];  act 1: pre[r][c] = v (if pre), v = GELU(v);  act 2: v *= GELU'(pre[r][c])
  *   C_f32[r][c] = v; C_bf16[r][c] = bf16(v); CT_bf16[c][r] = bf16(v); bias_grad[c] += sum_r v
  * (every output optional, at least one given). A, B 16-byte aligned, K % 8 == 0; row-major
- * outputs use ldc >= N, the transposed one ldt >= M. Stream-ordered; a pipeline wait that runs
- * out sets the context's device status word (bb_device_status). */
+ * outputs use ldc >= N, the transposed one ldt >= M. kt_per > 0 splits K into chunks of
+ * kt_per x 64 computed by different CTAs and added into C_f32 atomically (the caller zeroes it;
+ * no other output allowed); 0 = no split. Stream-ordered; a pipeline wait that runs out sets
+ * the context's device status word (bb_device_status). */
 int bb_gemm_bf16(bb_ctx* ctx, int64_t M, int N, int K, const void* A, const void* B,
                  float alpha, const float* bias, int act, float* pre, float* C_f32,
-                 void* C_bf16, void* CT_bf16, float* bias_grad, int ldc, int ldt, void* stream);
+                 void* C_bf16, void* CT_bf16, float* bias_grad, int ldc, int ldt, int kt_per,
+                 void* stream);
 
 /* Reads and clears the context's device status word (synchronises the stream); *out = 0 when
  * no kernel reported a problem, bit 0 = a corrupt connectivity entry, bit 1 = a wait ran out. */

@@ -19,8 +19,11 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
 
 
+# shapes cover both tile widths (BN 256 when it pads no more than 128), ragged M, N and K,
+# and more tiles than SMs (persistent CTAs cycling both TMEM accumulators)
 @pytest.mark.parametrize("M,N,K", [(128, 128, 64), (300, 200, 840), (1000, 512, 512),
-                                   (130, 336, 24), (4096, 840, 512)])
+                                   (130, 336, 24), (4096, 840, 512), (8192, 1024, 192),
+                                   (8192, 336, 520), (24576, 512, 840)])
 def test_gemm_plain(cuda, M, N, K):
     import torch
     from bbdg import mlp
@@ -33,6 +36,21 @@ def test_gemm_plain(cuda, M, N, K):
     torch.cuda.synchronize()
     assert _rel(C.cpu(), ref.cpu()) < 1e-5
     assert mlp.device_status() == 0
+
+
+@pytest.mark.parametrize("M,N,K", [(512, 512, 8192), (336, 512, 24576)])
+def test_gemm_split_k_through_mlp_shapes(cuda, M, N, K):
+    """Weight-gradient shapes (K = batch): the split-K path adds partial tiles atomically."""
+    import torch
+    from bbdg import mlp
+    g = torch.Generator(device="cuda").manual_seed(K)
+    A = torch.randn((M, K), generator=g, device=cuda).bfloat16()
+    B = torch.randn((N, K), generator=g, device=cuda).bfloat16()
+    C = torch.zeros((M, N), device=cuda)
+    mlp.gemm_bf16(A, B, out_f32=C, kt_per=16)
+    ref = A.double() @ B.double().T
+    torch.cuda.synchronize()
+    assert _rel(C.cpu(), ref.cpu()) < 1e-5
 
 
 def test_gemm_epilogues(cuda):
