@@ -122,17 +122,17 @@ class Closure:
         res.zero_()
         self.lo.run(q, res, self.dt_lo, self.lo_steps)
 
-    def correct(self, q: torch.Tensor) -> None:
-        """q += MLP(features(q)) / s_out."""
+    def correct(self, q: torch.Tensor, weight: float = 1.0) -> None:
+        """q += weight * MLP(features(q)) / s_out."""
         closure_features(self.cfg.N_lo, NF, self.lo.conn, q, self.s_in, X=self._X)
         self.net.forward(self._X, out=self._Y)
-        closure_apply(self.cfg.N_lo, NF, 1.0 / self.s_out, self._Y, q)
+        closure_apply(self.cfg.N_lo, NF, weight / self.s_out, self._Y, q)
 
-    def run_lo(self, q: torch.Tensor, nmacro: int, closure: bool) -> None:
+    def run_lo(self, q: torch.Tensor, nmacro: int, closure: bool, weight: float = 1.0) -> None:
         for _ in range(nmacro):
             self.plain_macro(q)
             if closure:
-                self.correct(q)
+                self.correct(q, weight)
 
     # ---- data ----------------------------------------------------------------------------
     def snapshots(self, seed: int, nmacro: int, rollout: bool = False, noise: float = 0.0):
@@ -254,7 +254,8 @@ class Closure:
         r = self.lo.mass_norms(b)
         return float(math.sqrt(np.sum(e) / max(np.sum(r), 1e-300)))
 
-    def evaluate(self, seed: int, nmacro: int, reference_dtype=torch.float64) -> dict:
+    def evaluate(self, seed: int, nmacro: int, reference_dtype=torch.float64,
+                 weights=(1.0,)) -> dict:
         """Errors at t = nmacro * macro against the FP64 degree-N_hi run reduced to N_lo, and
         wall times (CUDA events) of the plain N_hi, plain N_lo and closure N_lo runs."""
         ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
@@ -288,11 +289,13 @@ class Closure:
         out = {"seed": seed, "t_final": nmacro * self.macro, "hi_steps": self.cfg.hi_steps * nmacro,
                "lo_steps": self.lo_steps * nmacro, "hi_seconds": t_hi,
                "err_hi_vs_fp64_hi": err_hi_full, "err_hi_reduced": err_hi}
-        for name, cl in (("plain", False), ("closure", True)):
+        runs = [("plain", False, 1.0), ("closure", True, 1.0)]
+        runs += [(f"closure_w{w:g}", True, float(w)) for w in weights if w != 1.0]
+        for name, cl, w in runs:
             q5 = c0.clone()
-            self.run_lo(q5.clone(), 1, cl)  # warm
+            self.run_lo(q5.clone(), 1, cl, w)  # warm
             e0.record()
-            self.run_lo(q5, nmacro, cl)
+            self.run_lo(q5, nmacro, cl, w)
             e1.record()
             torch.cuda.synchronize()
             out[f"{name}_lo_seconds"] = e0.elapsed_time(e1) / 1e3

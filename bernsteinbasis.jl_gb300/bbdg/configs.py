@@ -210,7 +210,7 @@ def config5(n: int = 16, n_train: int = 16, nmacro_train: int = 40, epochs: int 
     print(json.dumps({"train": info}), flush=True)
     rows = []
     for s in eval_seeds:
-        r = cl.evaluate(s, nmacro_eval)
+        r = cl.evaluate(s, nmacro_eval, weights=(1.0, 0.5, 0.25))
         r.update(cl.apriori(s, nmacro_eval))
         rows.append(r)
         print(json.dumps(r), flush=True)

@@ -6,7 +6,8 @@ Prints one JSON line per shape: our kernel's time and TFLOP/s with an FP32 and w
 output, cuBLAS (torch.matmul, BF16 output) on the same operands for comparison, and the
 fraction of the measured dense BF16 peak (MEASURED_PEAKS.json, burst figure). Then one line
 for a whole closure-MLP training step (forward, backward, Adam) and one for inference at
-24,576 rows. Inputs are seeded random; timings are CUDA events after warm-up.
+24,576 rows. Inputs are seeded random; timings are CUDA events after warm-up, around a
+CUDA graph of `reps` calls (device time) except for the training step (host loop).
 """
 from __future__ import annotations
 
@@ -32,11 +33,29 @@ def _peak_tflops():
         return 1900.0, "fallback"
 
 
-def _time(fn, reps):
+def _time(fn, reps, graph=True):
+    """Milliseconds per call. With graph=True the calls are captured once into a CUDA graph
+    and replayed, so the figure is device time without the host's per-call overhead."""
     for _ in range(3):
         fn()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if graph:
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                for _ in range(reps):
+                    fn()
+        torch.cuda.current_stream().wait_stream(s)
+        g.replay()
+        torch.cuda.synchronize()
+        e0.record()
+        g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
     e0.record()
     for _ in range(reps):
         fn()
@@ -54,7 +73,7 @@ def run(shapes, reps=20, cublas=True):
         B = torch.randn((N, K), generator=g, device="cuda").bfloat16()
         C = torch.zeros((M, N), device="cuda")
         Cb = torch.empty((M, N), device="cuda", dtype=torch.bfloat16)
-        split = K >= 8192  # the weight-gradient shapes (K = batch) use split-K
+        split = K >= 8192 and M <= 1024  # the weight-gradient shapes (K = batch) split K
         kt = 16 if split else 0
         f = 2.0 * M * N * K
         ms = _time(lambda: mlp.gemm_bf16(A, B, out_f32=C, kt_per=kt), reps)
@@ -86,7 +105,7 @@ def mlp_step(batch=24576, dims=(840, 512, 512, 336), reps=10):
         Y = net.forward(X, XT, train=True)
         net.backward(Y, T)
         net.step(1e-4)
-    ms = _time(step, reps)
+    ms = _time(step, reps, graph=False)
     msi = _time(lambda: net.forward(X), reps)
     out = {"mlp": list(dims), "batch": batch, "train_step_ms": ms,
            "train_tflops": 3 * flops / ms / 1e9, "infer_ms": msi, "infer_tflops": flops / msi / 1e9}

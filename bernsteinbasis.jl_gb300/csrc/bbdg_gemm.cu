@@ -132,6 +132,158 @@ __device__ __forceinline__ float gelu_grad(float x) {
          x * 0.39894228040143268f * expf(-0.5f * x * x);
 }
 
+// Epilogue variants fixed at compile time (F != 0); F == 0 reads every option at run time.
+enum : int {
+  kBias = 1,      // v += bias[c]
+  kAct1 = 2,      // Pre = v (if kPreW), v = GELU(v)
+  kAct2 = 4,      // v *= GELU'(Pre)
+  kPreW = 8,      // store the pre-activation
+  kCf = 16,       // Cf = v
+  kCfAdd = 32,    // Cf += v atomically (split-K)
+  kCb = 64,       // Cb = bf16(v)
+  kBgrad = 128,   // bias_grad[c] += sum over rows of v
+};
+constexpr int kEpiMlpHiddenTrain = kBias | kAct1 | kPreW | kCb;
+constexpr int kEpiMlpHidden = kBias | kAct1 | kCb;
+constexpr int kEpiBiasF32 = kBias | kCf;
+constexpr int kEpiGeluGradBf16 = kAct2 | kCb | kBgrad;
+constexpr int kEpiGeluGrad = kAct2 | kBgrad;
+constexpr int kEpiSplitK = kCfAdd;
+constexpr int kEpiF32 = kCf;
+constexpr int kEpiBf16 = kCb;
+
+__device__ __forceinline__ void st_bf16x4(__nv_bfloat16* p, float4 v) {
+  __nv_bfloat162 lo = __floats2bfloat162_rn(v.x, v.y), hi = __floats2bfloat162_rn(v.z, v.w);
+  uint2 u;
+  u.x = *reinterpret_cast<uint32_t*>(&lo);
+  u.y = *reinterpret_cast<uint32_t*>(&hi);
+  *reinterpret_cast<uint2*>(p) = u;
+}
+
+// One element of the epilogue with compile-time options.
+template <int F>
+__device__ __forceinline__ float epi_value(float x, float b, const GemmEpilogue& ep, size_t off) {
+  if (F & kBias) x += b;
+  if (F & kAct1) {
+    if (F & kPreW) ep.Pre[off] = x;
+    x = gelu(x);
+  }
+  if (F & kAct2) x *= gelu_grad(ep.Pre[off]);
+  return x;
+}
+
+// Row pass of a staged 32 x 32 chunk (T, pitch 36 floats) with compile-time options: lane l
+// handles columns c0 + 4 (l % 8) .. + 3 of rows 4 i + l / 8, so one warp store writes four
+// contiguous 128-byte (FP32) or 64-byte (BF16) row segments. vec: every output row start is
+// 16-byte aligned (ldc % 4 == 0 and aligned bases), else the lane falls back to scalars.
+template <int F>
+__device__ __forceinline__ void epi_rows(const GemmEpilogue& ep, float* T, int r0, int c0,
+                                         int rows, int lane, bool vec) {
+  const int q = lane >> 3, cg = (lane & 7) * 4;
+  const int c = c0 + cg;
+  const int ncol = min(4, ep.N - c);  // columns of this lane inside the matrix (may be <= 0)
+  float b[4] = {0.f, 0.f, 0.f, 0.f};
+  if (F & kBias) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (j < ncol) b[j] = ep.bias[c + j];
+  }
+  float g[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int rr = 4 * i + q;
+    float4 x4 = *reinterpret_cast<const float4*>(T + rr * 36 + cg);
+    if (rr < rows && ncol > 0) {
+      const size_t off = (size_t)(r0 + rr) * ep.ldc + c;
+      float x[4] = {ep.alpha * x4.x, ep.alpha * x4.y, ep.alpha * x4.z, ep.alpha * x4.w};
+      if (vec && ncol == 4) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          if (F & kBias) x[j] += b[j];
+        }
+        if (F & kAct2) {
+          const float4 p4 = *reinterpret_cast<const float4*>(ep.Pre + off);
+          const float pr[4] = {p4.x, p4.y, p4.z, p4.w};
+#pragma unroll
+          for (int j = 0; j < 4; ++j) x[j] *= gelu_grad(pr[j]);
+        }
+        if (F & kAct1) {
+          if (F & kPreW) *reinterpret_cast<float4*>(ep.Pre + off) = make_float4(x[0], x[1], x[2], x[3]);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) x[j] = gelu(x[j]);
+        }
+        x4 = make_float4(x[0], x[1], x[2], x[3]);
+        if (F & kCf) *reinterpret_cast<float4*>(ep.Cf + off) = x4;
+        if (F & kCfAdd) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j) atomicAdd(ep.Cf + off + j, x[j]);
+        }
+        if (F & kCb) st_bf16x4(ep.Cb + off, x4);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          if (j < ncol) {
+            x[j] = epi_value<F>(x[j], b[j], ep, off + j);
+            if (F & kCf) ep.Cf[off + j] = x[j];
+            if (F & kCfAdd) atomicAdd(ep.Cf + off + j, x[j]);
+            if (F & kCb) ep.Cb[off + j] = __float2bfloat16_rn(x[j]);
+          }
+        }
+        x4 = make_float4(x[0], x[1], x[2], x[3]);
+      }
+      if (F & kBgrad) {
+        g[0] += x4.x;
+        g[1] += x4.y;
+        g[2] += x4.z;
+        g[3] += x4.w;
+      }
+      *reinterpret_cast<float4*>(T + rr * 36 + cg) = x4;
+    }
+  }
+  if (F & kBgrad) {
+    // lanes l, l+8, l+16, l+24 hold the same columns
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      g[j] += __shfl_xor_sync(0xffffffffu, g[j], 8);
+      g[j] += __shfl_xor_sync(0xffffffffu, g[j], 16);
+    }
+    if (q == 0) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (j < ncol) atomicAdd(ep.bias_grad + c + j, g[j]);
+    }
+  }
+}
+
+// Row pass with every option read at run time (any alignment, any combination).
+__device__ __forceinline__ void epi_rows_generic(const GemmEpilogue& ep, float* T, int r0,
+                                                 int c0, int rows, int lane, bool split) {
+  const int c = c0 + lane;
+  const bool cin = c < ep.N;
+  const float b = (cin && ep.bias) ? ep.bias[c] : 0.0f;
+  float gsum = 0.0f;
+  for (int rr = 0; rr < rows; ++rr) {
+    float x = ep.alpha * T[rr * 36 + lane] + b;
+    if (cin) {
+      const size_t off = (size_t)(r0 + rr) * ep.ldc + c;
+      if (ep.act == 1) {
+        if (ep.Pre) ep.Pre[off] = x;
+        x = gelu(x);
+      } else if (ep.act == 2) {
+        x *= gelu_grad(ep.Pre[off]);
+      }
+      if (ep.Cf) {
+        if (split) atomicAdd(ep.Cf + off, x);
+        else ep.Cf[off] = ep.accumulate ? ep.Cf[off] + x : x;
+      }
+      if (ep.Cb) ep.Cb[off] = __float2bfloat16_rn(x);
+      gsum += x;
+    }
+    T[rr * 36 + lane] = x;
+  }
+  if (ep.bias_grad && cin) atomicAdd(ep.bias_grad + c, gsum);
+}
+
 template <int BN_>
 struct GemmCfg {
   static constexpr int BM = 128, BN = BN_, BK = 64, UMMA_K = 16;
@@ -142,7 +294,7 @@ struct GemmCfg {
   static constexpr int TMEM_COLS = 2 * BN;               // two FP32 accumulators
   static constexpr int EPI_WARPS = 4;
   static constexpr int THREADS = 64 + 32 * EPI_WARPS;
-  static constexpr int EPI_PITCH = 33;                   // floats; conflict-free both ways
+  static constexpr int EPI_PITCH = 36;                   // floats; 16-byte rows
   static constexpr int EPI_BYTES = EPI_WARPS * 32 * EPI_PITCH * 4;
   static constexpr int NBAR = 2 * STAGES + 5;
   static constexpr int SMEM = STAGES * STAGE_BYTES + EPI_BYTES + 8 * NBAR + 16 + 1024;
@@ -169,7 +321,7 @@ struct TileSched {
 
 __device__ __forceinline__ bool flag_set(const volatile int* f) { return *f != 0; }
 
-template <int BN>
+template <int BN, int F>
 __global__ void __launch_bounds__(GemmCfg<BN>::THREADS, 1)
     gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tmA,
                         const __grid_constant__ CUtensorMap tmB, GemmEpilogue ep, TileSched ts) {
@@ -284,6 +436,9 @@ __global__ void __launch_bounds__(GemmCfg<BN>::THREADS, 1)
   } else {
     // ---- epilogue warps ----
     const int g = warp & 3;  // TMEM lane quarter this warp may access
+    // 16-byte vector stores need 16-byte aligned row starts for every row-major output
+    const bool vec = (ep.ldc % 4 == 0) && ((((uintptr_t)ep.Cf | (uintptr_t)ep.Pre) & 15) == 0) &&
+                     ((((uintptr_t)ep.Cb) & 7) == 0);
     float* T = epi + (warp - 2) * 32 * C::EPI_PITCH;
     int local = 0;
     for (int tile = blockIdx.x; tile < total; tile += gridDim.x, ++local) {
@@ -314,41 +469,22 @@ __global__ void __launch_bounds__(GemmCfg<BN>::THREADS, 1)
           if (lane == 0) mbar_arrive(&tempty[a]);
         }
         if (n0 + c0 >= ep.N) continue;
+        // stage the chunk: lane = row, 8 x 16-byte stores (conflict-free with pitch 36)
 #pragma unroll
-        for (int j = 0; j < 32; ++j) T[lane * C::EPI_PITCH + j] = v[j];
+        for (int j = 0; j < 32; j += 4)
+          *reinterpret_cast<float4*>(T + lane * C::EPI_PITCH + j) =
+              make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
         __syncwarp();
-        // row pass: lane owns column c; each store covers one contiguous row segment
-        const int c = n0 + c0 + lane;
-        const bool cin = c < ep.N;
-        const float b = (cin && ep.bias) ? ep.bias[c] : 0.0f;
-        float gsum = 0.0f;
         const int rows = min(32, ep.M - r0);
-        for (int rr = 0; rr < rows; ++rr) {
-          float x = fmaf(ep.alpha, T[rr * C::EPI_PITCH + lane], b);
-          if (cin) {
-            const size_t off = (size_t)(r0 + rr) * ep.ldc + c;
-            if (ep.act == 1) {
-              if (ep.Pre) ep.Pre[off] = x;
-              x = gelu(x);
-            } else if (ep.act == 2) {
-              x *= gelu_grad(ep.Pre[off]);
-            }
-            if (ep.Cf) {
-              if (ep.kt_per < ts.nkt_all) atomicAdd(ep.Cf + off, x);
-              else ep.Cf[off] = ep.accumulate ? ep.Cf[off] + x : x;
-            }
-            if (ep.Cb) ep.Cb[off] = __float2bfloat16_rn(x);
-            gsum += x;
-          }
-          T[rr * C::EPI_PITCH + lane] = x;
-        }
-        if (ep.bias_grad && cin) atomicAdd(ep.bias_grad + c, gsum);
+        if (F == 0) epi_rows_generic(ep, T, r0, n0 + c0, rows, lane, ep.kt_per < ts.nkt_all);
+        else epi_rows<F>(ep, T, r0, n0 + c0, rows, lane, vec);
         if (ep.CbT) {
           // column pass: lane owns row r0 + lane; each store covers one column segment
           __syncwarp();
           if (lane < rows) {
             const int cols = min(32, ep.N - (n0 + c0));
             __nv_bfloat16* o = ep.CbT + (size_t)(n0 + c0) * ep.ldt + r0 + lane;
+#pragma unroll 8
             for (int j = 0; j < cols; ++j)
               o[(size_t)j * ep.ldt] = __float2bfloat16_rn(T[lane * C::EPI_PITCH + j]);
           }
@@ -405,27 +541,62 @@ int make_map(bb_ctx* ctx, CUtensorMap* tm, const void* ptr, int64_t rows, int K,
   return BB_OK;
 }
 
-template <int BN>
-int launch_bn(bb_ctx* ctx, const CUtensorMap& ta, const void* B, int N, int K, GemmEpilogue ep,
-              TileSched ts, cudaStream_t st) {
+template <int BN, int F>
+int launch_bnf(bb_ctx* ctx, const CUtensorMap& ta, const CUtensorMap& tb, GemmEpilogue ep,
+               TileSched ts, cudaStream_t st) {
   using C = GemmCfg<BN>;
-  CUtensorMap tb;
-  int rc = make_map(ctx, &tb, B, N, K, BN);
-  if (rc) return rc;
   static std::mutex attr_mu;
   static uint64_t attr_done = 0;  // one bit per device
   {
     std::lock_guard<std::mutex> lock(attr_mu);
     const uint64_t bit = 1ull << (ctx->device & 63);
     if (!(attr_done & bit)) {
-      BB_CUDA(ctx, cudaFuncSetAttribute(gemm_bf16_tn_kernel<BN>,
+      BB_CUDA(ctx, cudaFuncSetAttribute(gemm_bf16_tn_kernel<BN, F>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
       attr_done |= bit;
     }
   }
   const int grid = std::min(ts.total(), ctx->num_sms);
-  gemm_bf16_tn_kernel<BN><<<grid, C::THREADS, C::SMEM, st>>>(ta, tb, ep, ts);
+  gemm_bf16_tn_kernel<BN, F><<<grid, C::THREADS, C::SMEM, st>>>(ta, tb, ep, ts);
   return bb_check_launch(ctx, "gemm_bf16_tn_kernel");
+}
+
+// The compile-time epilogue matching the requested outputs, 0 (run-time options) if none.
+int epilogue_variant(const GemmEpilogue& ep, bool split) {
+  int f = 0;
+  if (ep.bias) f |= kBias;
+  if (ep.act == 1) f |= kAct1 | (ep.Pre ? kPreW : 0);
+  if (ep.act == 2) f |= kAct2;
+  if (ep.Cf) f |= split ? kCfAdd : (ep.accumulate ? 0 : kCf);
+  if (ep.Cf && ep.accumulate && !split) return 0;
+  if (ep.Cb) f |= kCb;
+  if (ep.bias_grad) f |= kBgrad;
+  switch (f) {
+    case kEpiMlpHiddenTrain: case kEpiMlpHidden: case kEpiBiasF32: case kEpiGeluGradBf16:
+    case kEpiGeluGrad: case kEpiSplitK: case kEpiF32: case kEpiBf16:
+      return f;
+    default:
+      return 0;
+  }
+}
+
+template <int BN>
+int launch_bn(bb_ctx* ctx, const CUtensorMap& ta, const void* B, int N, int K, GemmEpilogue ep,
+              TileSched ts, cudaStream_t st) {
+  CUtensorMap tb;
+  int rc = make_map(ctx, &tb, B, N, K, BN);
+  if (rc) return rc;
+  switch (epilogue_variant(ep, ts.splits > 1)) {
+    case kEpiMlpHiddenTrain: return launch_bnf<BN, kEpiMlpHiddenTrain>(ctx, ta, tb, ep, ts, st);
+    case kEpiMlpHidden: return launch_bnf<BN, kEpiMlpHidden>(ctx, ta, tb, ep, ts, st);
+    case kEpiBiasF32: return launch_bnf<BN, kEpiBiasF32>(ctx, ta, tb, ep, ts, st);
+    case kEpiGeluGradBf16: return launch_bnf<BN, kEpiGeluGradBf16>(ctx, ta, tb, ep, ts, st);
+    case kEpiGeluGrad: return launch_bnf<BN, kEpiGeluGrad>(ctx, ta, tb, ep, ts, st);
+    case kEpiSplitK: return launch_bnf<BN, kEpiSplitK>(ctx, ta, tb, ep, ts, st);
+    case kEpiF32: return launch_bnf<BN, kEpiF32>(ctx, ta, tb, ep, ts, st);
+    case kEpiBf16: return launch_bnf<BN, kEpiBf16>(ctx, ta, tb, ep, ts, st);
+    default: return launch_bnf<BN, 0>(ctx, ta, tb, ep, ts, st);
+  }
 }
 
 }  // namespace

@@ -77,9 +77,9 @@ struct FastLayout {
   static constexpr int SLOT = ((QBYTES + GEOBYTES + CONNBYTES) + 15) / 16 * 16;
   static constexpr int RES_B = 2 * SLOT;                       // after the two q slots
   static constexpr int G_B = RES_B + QBYTES;                   // [NCHAIN][NPS] face stacks
-  static constexpr int W_B = G_B + (NCHAIN * NPS * 4 + 15) / 16 * 16;  // [NW][EPB][NPM1P]
-  static constexpr int VOL_B = W_B + (NW * EPB * NPM1P * 4 + 15) / 16 * 16;  // [NW][EPB][NP]
-  static constexpr int GA_B = VOL_B + NW * EPB * NP * 4;       // [NP] uint4
+  static constexpr int X_B = G_B + (NCHAIN * NPS * 4 + 15) / 16 * 16;  // [2][NCHAIN][NFP]
+  static constexpr int W_B = X_B + (2 * NCHAIN * NFP * 4 + 15) / 16 * 16;  // [NW][EPB][NPM1P]
+  static constexpr int GA_B = W_B + (NW * EPB * NPM1P * 4 + 15) / 16 * 16;  // [NP] uint4
   static constexpr int GW_B = GA_B + NP * 16;                  // [NP] float4 alpha_b
   static constexpr int LW_B = GW_B + NP * 16;                  // [NP] float4 l_d per face
   static constexpr int VN_B = LW_B + NP * 16;                  // [NPM1] uint2
@@ -196,7 +196,7 @@ __device__ __forceinline__ void lift_chain(const float* x, float* g) {
 }
 
 template <int N, int PHYS, int EPB, int TPE>
-__global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT)
+__global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT, 2)
     stage_fast_kernel(FastStageParams P) {
   using L = FastLayout<N, PHYS, EPB, TPE>;
   constexpr int NP = L::NP, NFP = L::NFP, NPM1 = L::NPM1, NF = L::NF, NCH = L::NCH;
@@ -208,8 +208,8 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT)
   extern __shared__ __align__(16) unsigned char smem[];
   float* sRes = reinterpret_cast<float*>(smem + L::RES_B);
   float* sG = reinterpret_cast<float*>(smem + L::G_B);
+  float* sX = reinterpret_cast<float*>(smem + L::X_B);  // chain inputs, two tiles
   float* sW = reinterpret_cast<float*>(smem + L::W_B);
-  float* sVol = reinterpret_cast<float*>(smem + L::VOL_B);
   // per coefficient alpha: degree N-1 indices of alpha - e_b (NPM1 = zero entry when
   // alpha_b = 0) and face-stack positions; alpha_b; l_d of its layer on each face
   uint4* sGA = reinterpret_cast<uint4*>(smem + L::GA_B);
@@ -221,6 +221,7 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT)
   // partner face nf, orientation o, node a -> volume index of the partner's node
   uint16_t* sFnb = reinterpret_cast<uint16_t*>(smem + L::FNB_B);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L::BAR_B);  // [0],[1] q slots, [2] res
+  __shared__ int s_fail;
   const int tid = threadIdx.x;
   const int64_t K = P.K;
   const int64_t ntiles = K / EPB;  // the host guarantees K % EPB == 0
@@ -257,6 +258,7 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT)
   };
 
   if (tid == 0) {
+    s_fail = 0;
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     mbar_init(&bar[2], 1);
@@ -301,108 +303,113 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT)
     }
   }
   __syncthreads();
-  if (tid == 0 && (int64_t)blockIdx.x < ntiles) {
-    issue_main(blockIdx.x, 0);
-    if (stage) issue_res(blockIdx.x);
+  // the first two tiles of this block go to the two slots
+  const int64_t t0 = blockIdx.x;
+  if (tid == 0 && t0 < ntiles) {
+    issue_main(t0, 0);
+    if (stage) issue_res(t0);
+    if (t0 + gridDim.x < ntiles) issue_main(t0 + gridDim.x, 1);
   }
-  uint32_t ph = 0u;  // bit b: parity of the phase barrier b waits for next
-  bool failed = false;
+  uint32_t ph = 0u;  // bit b: parity of the phase barrier b waits for next (element threads)
   const float rkA = P.rkA, rkB = P.rkB, dt = P.dt, tau = P.tau;
   // face handled by this element thread in the flux and trace phases
   const int ff = u / FT, fa0 = u - (u / FT) * FT;
 
+  // interface flux of face ff of element le of tile t (q in slot s) -> chain inputs xbuf
+  auto flux_tile = [&](int64_t t, int s, float* xbuf) {
+    const int64_t e0 = t * EPB;
+    const float* sQ = slot_q(s);
+    const float* sGeo = slot_geo(s);
+    const int32_t* sConn = slot_conn(s);
+    const int32_t c = sConn[le * 4 + ff];
+    const int64_t nbr = (int64_t)((uint32_t)c >> 5);
+    const int nface = (c >> 3) & 3, o = c & 7;
+    const bool bad = nbr >= K || o > 5;
+    const bool inside = nbr >= e0 && nbr < e0 + EPB;
+    if (bad && fa0 == 0) atomicOr(P.status, 1);
+    const float* g = sGeo + le * BB_GEO_STRIDE;
+    const float nx = g[12 + ff], ny = g[16 + ff], nz = g[20 + ff];
+    float cp = 1.f, cu = 1.f;
+    if (tau > 0.f) {
+      const float n2 = nx * nx + ny * ny + nz * nz;
+      const float rJf = rsqrtf(n2);
+      cp = tau * n2 * rJf;  // tau |n|
+      cu = tau * rJf;       // tau / |n|
+    }
+    // outside-tile neighbour traces: issue every global load before using any
+    float tr[FR][NF];
+    const float* tbase = P.trace_in + ((size_t)(bad ? 0 : nbr) * 4 + nface) * NF * NFP;
+#pragma unroll
+    for (int r = 0; r < FR; ++r) {
+      const int a = fa0 + r * FT;
+      if (a < NFP && !inside && !bad) {
+        const float* tp = tbase + sFperm[o * NFP + a];
+#pragma unroll
+        for (int m = 0; m < NF; ++m) tr[r][m] = __ldg(tp + m * NFP);
+      }
+    }
+    const int pin = (int)(nbr - e0);
+    float* xin0 = xbuf + ((le * 4 + ff) * NCH) * NFP;
+#pragma unroll
+    for (int r = 0; r < FR; ++r) {
+      const int a = fa0 + r * FT;
+      if (a >= NFP) continue;
+      float d[NF];
+      const float* qM = sQ + le * NP + sFvol[ff * NFP + a];
+      if (bad) {
+#pragma unroll
+        for (int m = 0; m < NF; ++m) d[m] = 0.f;
+      } else if (inside) {
+        const float* qP = sQ + pin * NP + sFnb[(nface * 6 + o) * NFP + a];
+#pragma unroll
+        for (int m = 0; m < NF; ++m) d[m] = qP[m * EPB * NP] - qM[m * EPB * NP];
+      } else {
+#pragma unroll
+        for (int m = 0; m < NF; ++m) d[m] = tr[r][m] - qM[m * EPB * NP];
+      }
+      float* xin = xin0 + a;
+      if constexpr (PHYS == BB_WAVE) {
+        const float ndotdU = nx * d[1] + ny * d[2] + nz * d[3];
+        xin[0] = 0.5f * (cp * d[0] - ndotdU);    // p flux
+        xin[NFP] = 0.5f * (cu * ndotdU - d[0]);  // (u,v,w) flux / n
+      } else {
+        const float Hx = d[0], Hy = d[1], Hz = d[2], Ex = d[3], Ey = d[4], Ez = d[5];
+        const float ndH = nx * Hx + ny * Hy + nz * Hz;
+        const float ndE = nx * Ex + ny * Ey + nz * Ez;
+        const float ax[6] = {0.f, Ez, -Ey, 0.f, -Hz, Hy};
+        const float ay[6] = {-Ez, 0.f, Ex, Hz, 0.f, -Hx};
+        const float az[6] = {Ey, -Ex, 0.f, -Hy, Hx, 0.f};
+        const float nd[6] = {ndH * nx, ndH * ny, ndH * nz, ndE * nx, ndE * ny, ndE * nz};
+#pragma unroll
+        for (int m = 0; m < 6; ++m)
+          xin[m * NFP] = 0.5f * ax[m] * nx + 0.5f * ay[m] * ny + 0.5f * az[m] * nz +
+                         0.5f * (cp * d[m]) - 0.5f * (cu * nd[m]);
+      }
+    }
+  };
+
+  // prologue: flux of the first tile
+  if (is_elem && t0 < ntiles) {
+    if (!mbar_wait(&bar[0], 0u)) s_fail = 1;
+    ph ^= 1u;
+    flux_tile(t0, 0, sX);
+  }
+  __syncthreads();
+
   int it = 0;
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+  for (int64_t tile = t0; tile < ntiles && !s_fail; tile += gridDim.x, ++it) {
     const int s = it & 1;
     const int64_t e0 = tile * EPB;
     const int64_t tnext = tile + gridDim.x;
     float* sQ = slot_q(s);
     const float* sGeo = slot_geo(s);
     const int32_t* sConn = slot_conn(s);
-    // ---- 1. wait for this tile, prefetch the next one into the other slot ------------
-    failed = __syncthreads_or(!mbar_wait(&bar[s], (ph >> s) & 1u));
-    if (failed) break;
-    ph ^= 1u << s;
-    if (tid == 0 && tnext < ntiles) {
-      tma_store_wait_read();  // bulk stores of the other slot have read it
-      fence_async_smem();
-      issue_main(tnext, s ^ 1);
-    }
 
-    // ---- 2. interface flux of face ff of element le -> chain inputs -------------------
-    if (is_elem) {
-      const int32_t c = sConn[le * 4 + ff];
-      const int64_t nbr = (int64_t)((uint32_t)c >> 5);
-      const int nface = (c >> 3) & 3, o = c & 7;
-      const bool bad = nbr >= K || o > 5;
-      const bool inside = nbr >= e0 && nbr < e0 + EPB;
-      if (bad && fa0 == 0) atomicOr(P.status, 1);
-      const float* g = sGeo + le * BB_GEO_STRIDE;
-      const float nx = g[12 + ff], ny = g[16 + ff], nz = g[20 + ff];
-      float cp = 1.f, cu = 1.f;
-      if (tau > 0.f) {
-        const float n2 = nx * nx + ny * ny + nz * nz;
-        const float rJf = rsqrtf(n2);
-        cp = tau * n2 * rJf;  // tau |n|
-        cu = tau * rJf;       // tau / |n|
-      }
-      // outside-tile neighbour traces: issue every global load before using any
-      float tr[FR][NF];
-      const float* tbase = P.trace_in + ((size_t)(bad ? 0 : nbr) * 4 + nface) * NF * NFP;
-#pragma unroll
-      for (int r = 0; r < FR; ++r) {
-        const int a = fa0 + r * FT;
-        if (a < NFP && !inside && !bad) {
-          const float* tp = tbase + sFperm[o * NFP + a];
-#pragma unroll
-          for (int m = 0; m < NF; ++m) tr[r][m] = __ldg(tp + m * NFP);
-        }
-      }
-      const int pin = (int)(nbr - e0);
-      float* xin0 = sG + ((le * 4 + ff) * NCH) * NPS + (NPS - NFP);
-#pragma unroll
-      for (int r = 0; r < FR; ++r) {
-        const int a = fa0 + r * FT;
-        if (a >= NFP) continue;
-        float d[NF];
-        const float* qM = sQ + le * NP + sFvol[ff * NFP + a];
-        if (bad) {
-#pragma unroll
-          for (int m = 0; m < NF; ++m) d[m] = 0.f;
-        } else if (inside) {
-          const float* qP = sQ + pin * NP + sFnb[(nface * 6 + o) * NFP + a];
-#pragma unroll
-          for (int m = 0; m < NF; ++m) d[m] = qP[m * EPB * NP] - qM[m * EPB * NP];
-        } else {
-#pragma unroll
-          for (int m = 0; m < NF; ++m) d[m] = tr[r][m] - qM[m * EPB * NP];
-        }
-        float* xin = xin0 + a;
-        if constexpr (PHYS == BB_WAVE) {
-          const float ndotdU = nx * d[1] + ny * d[2] + nz * d[3];
-          xin[0] = 0.5f * (cp * d[0] - ndotdU);    // p flux
-          xin[NPS] = 0.5f * (cu * ndotdU - d[0]);  // (u,v,w) flux / n
-        } else {
-          const float Hx = d[0], Hy = d[1], Hz = d[2], Ex = d[3], Ey = d[4], Ez = d[5];
-          const float ndH = nx * Hx + ny * Hy + nz * Hz;
-          const float ndE = nx * Ex + ny * Ey + nz * Ez;
-          const float ax[6] = {0.f, Ez, -Ey, 0.f, -Hz, Hy};
-          const float ay[6] = {-Ez, 0.f, Ex, Hz, 0.f, -Hx};
-          const float az[6] = {Ey, -Ex, 0.f, -Hy, Hx, 0.f};
-          const float nd[6] = {ndH * nx, ndH * ny, ndH * nz, ndE * nx, ndE * ny, ndE * nz};
-#pragma unroll
-          for (int m = 0; m < 6; ++m)
-            xin[m * NPS] = 0.5f * ax[m] * nx + 0.5f * ay[m] * ny + 0.5f * az[m] * nz +
-                           0.5f * (cp * d[m]) - 0.5f * (cu * nd[m]);
-        }
-      }
-    }
-    __syncthreads();
-
-    // ---- 3. chain warps: lift chains || element threads: volume term -----------------
+    // ---- A. chain warps: lift chains of this tile || element threads: volume term of
+    //         this tile, then the interface flux of the next tile -------------------------
     if (!is_elem) {
       const int c = tid - NTE;
-      if (c < NCHAIN) lift_chain<N>(sG + c * NPS + (NPS - NFP), sG + c * NPS);
+      if (c < NCHAIN) lift_chain<N>(sX + (s * NCHAIN + c) * NFP, sG + c * NPS);
     } else {
       const float* g = sGeo + le * BB_GEO_STRIDE;
       // barycentric weights of J d/dx, J d/dy, J d/dz: g_a = (rxJ, sxJ, txJ, -sum)/2; the
@@ -411,7 +418,7 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT)
       const float gy[3] = {0.5f * g[3], 0.5f * g[4], 0.5f * g[5]};
       const float gz[3] = {0.5f * g[6], 0.5f * g[7], 0.5f * g[8]};
       const float* q0 = sQ + le * NP;
-      // 3a. w(beta) at degree N-1
+      // w(beta) at degree N-1; vol(alpha) = sum_b alpha_b w(alpha - e_b) is formed in B
 #pragma unroll
       for (int r = 0; r < VR; ++r) {
         const int b = u + r * TPE;
@@ -456,32 +463,20 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT)
 #pragma unroll
         for (int m = 0; m < NW; ++m) sW[(m * EPB + le) * L::NPM1P + b] = w[m];
       }
-      named_sync(1, NTE);
-      // 3b. vol(alpha) = sum_b alpha_b w(alpha - e_b), the volume part of J * rhs
-      const float* wb = sW + le * L::NPM1P;
-#pragma unroll
-      for (int r = 0; r < GR; ++r) {
-        const int n = u + r * TPE;
-        if (n >= NP) continue;
-        const uint4 ga = sGA[n];
-        const float4 gw4 = sGW[n];
-        const int x0 = ga.x & 0xffff, x1 = ga.x >> 16, x2 = ga.y & 0xffff, x3 = ga.y >> 16;
-#pragma unroll
-        for (int m = 0; m < NW; ++m) {
-          const float* wm = wb + m * EPB * L::NPM1P;
-          sVol[(m * EPB + le) * NP + n] =
-              fmaf(gw4.x, wm[x0], fmaf(gw4.y, wm[x1], fmaf(gw4.z, wm[x2], gw4.w * wm[x3])));
-        }
+      if (tnext < ntiles) {
+        if (!mbar_wait(&bar[s ^ 1], (ph >> (s ^ 1)) & 1u)) s_fail = 1;
+        ph ^= 1u << (s ^ 1);
+        flux_tile(tnext, s ^ 1, sX + (s ^ 1) * NCHAIN * NFP);
+      }
+      if (stage) {
+        if (!mbar_wait(&bar[2], (ph >> 2) & 1u)) s_fail = 1;
+        ph ^= 4u;
       }
     }
     __syncthreads();
-    if (stage) {
-      failed = __syncthreads_or(!mbar_wait(&bar[2], (ph >> 2) & 1u));
-      if (failed) break;
-      ph ^= 4u;
-    }
+    if (s_fail) break;
 
-    // ---- 4. sum lift stacks + volume term, divide by J, LSRK update ------------------
+    // ---- B. sum lift stacks + volume term, divide by J, LSRK update ------------------
     if (is_elem) {
       const float* g = sGeo + le * BB_GEO_STRIDE;
       const float invJ = g[9];
@@ -493,14 +488,23 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT)
         nzf[f] = g[20 + f];
       }
       const float* G = sG + le * 4 * NCH * NPS;
+      const float* wb = sW + le * L::NPM1P;
 #pragma unroll
       for (int r = 0; r < GR; ++r) {
         const int n = u + r * TPE;
         if (n >= NP) continue;
-        const uint32_t pos = sGA[n].w;
+        const uint4 ga = sGA[n];
+        const float4 gw4 = sGW[n];
         const float4 lw = sLW[n];
         const float lwf[4] = {lw.x, lw.y, lw.z, lw.w};
-        const int p[4] = {(int)(pos & 1023), (int)((pos >> 10) & 1023), (int)(pos >> 20), n};
+        const int p[4] = {(int)(ga.w & 1023), (int)((ga.w >> 10) & 1023), (int)(ga.w >> 20), n};
+        const int x0 = ga.x & 0xffff, x1 = ga.x >> 16, x2 = ga.y & 0xffff, x3 = ga.y >> 16;
+        float vol[NW];
+#pragma unroll
+        for (int m = 0; m < NW; ++m) {
+          const float* wm = wb + m * EPB * L::NPM1P;
+          vol[m] = fmaf(gw4.x, wm[x0], fmaf(gw4.y, wm[x1], fmaf(gw4.z, wm[x2], gw4.w * wm[x3])));
+        }
         float rhs[NF];
         if constexpr (PHYS == BB_WAVE) {
           // face order of src/BernsteinLift.jl:202-214: t=-1 face first, then f1, f2, f3
@@ -515,18 +519,17 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT)
             By = fmaf(nyf[f], Bf, By);
             Bz = fmaf(nzf[f], Bf, Bz);
           }
-          const float* vol = sVol + le * NP + n;
           rhs[0] = (A - vol[0]) * invJ;
-          rhs[1] = (Bx - vol[EPB * NP]) * invJ;
-          rhs[2] = (By - vol[2 * EPB * NP]) * invJ;
-          rhs[3] = (Bz - vol[3 * EPB * NP]) * invJ;
+          rhs[1] = (Bx - vol[1]) * invJ;
+          rhs[2] = (By - vol[2]) * invJ;
+          rhs[3] = (Bz - vol[3]) * invJ;
         } else {
 #pragma unroll
           for (int m = 0; m < 6; ++m) {
             float v = lwf[3] * G[(3 * 6 + m) * NPS + p[3]];
 #pragma unroll
             for (int f = 0; f < 3; ++f) v = fmaf(lwf[f], G[(f * 6 + m) * NPS + p[f]], v);
-            rhs[m] = (v + sVol[(m * EPB + le) * NP + n]) * invJ;
+            rhs[m] = (v + vol[m]) * invJ;
           }
         }
         const int item = le * NP + n;
@@ -545,7 +548,7 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT)
     }
     __syncthreads();
 
-    // ---- 5. write back q and res (bulk stores), then the outgoing traces -------------
+    // ---- C. write back q and res (bulk stores) and the outgoing traces ----------------
     if (stage) {
       if (tid == 0) {
         fence_async_smem();  // make the generic-proxy smem writes visible to the bulk copies
@@ -555,11 +558,6 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT)
           tma_store(P.res + ((size_t)m * K + e0) * NP, sRes + m * EPB * NP, EPB * NP * 4);
         }
         tma_store_commit();
-        if (tnext < ntiles) {
-          tma_store_wait_read();  // sRes has been read out; refill it for the next tile
-          fence_async_smem();
-          issue_res(tnext);
-        }
       }
       if (P.trace_out && is_elem) {
         const int64_t nbr = (int64_t)((uint32_t)sConn[le * 4 + ff] >> 5);
@@ -577,8 +575,19 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT)
       }
     }
     __syncthreads();
+    // refill: this slot takes the tile after next, the res buffer the next tile
+    if (tid == 0) {
+      const int64_t tnn = tnext + gridDim.x;
+      const bool more_q = tnn < ntiles, more_res = stage && tnext < ntiles;
+      if (more_q || more_res) {
+        tma_store_wait_read();  // the bulk stores have read this slot and the res buffer
+        fence_async_smem();
+        if (more_q) issue_main(tnn, s);
+        if (more_res) issue_res(tnext);
+      }
+    }
   }
-  if (failed && tid == 0) {
+  if (s_fail && tid == 0) {
     atomicOr(P.status, 2);
     // let copies still in flight land before the block exits (bounded)
     for (int b = 0; b < 3; ++b) mbar_wait(&bar[b], (ph >> b) & 1u);

@@ -1,0 +1,79 @@
+"""GPU: the learned closure end to end, at a reduced size (8^3 x 6 = 3,072 elements).
+
+Degree-10 Maxwell runs generate the data, the FP64 degree reduction maps them to degree 5,
+the MLP trains with the library's tcgen05 GEMM kernels, and held-out initial conditions
+measure what the network gains over the plain degree-5 solver. The gain asserted is the
+teacher-forced one (one macro step from the reduced degree-10 state, held-out seeds): it is
+the error the network removes per step. The free-running corrected solve is checked for
+finiteness and its error is reported, not asserted (the full-size results, with the
+rollout, are measured by `python -m bbdg.configs --config 5`).
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def trained(cuda, bb):
+    from bbdg.closure import Closure, ClosureConfig
+    mesh = bb.uniform_tet_mesh(8)
+    cl = Closure(mesh, ClosureConfig(N_hi=10, N_lo=5, hidden=(512, 512)), seed=3)
+    cl.fit_scales(101, 3)
+    info = cl.train([101 + i for i in range(8)], 40, epochs=10, lr=1e-3, lr_final=1e-5,
+                    noise=0.01)
+    return cl, info
+
+
+def test_training_loss_falls(trained):
+    cl, info = trained
+    loss = info["epoch_loss"]
+    assert all(math.isfinite(v) for v in loss)
+    assert loss[-1] < 0.8 * loss[0], loss
+
+
+def test_closure_gains_over_plain_solver_on_held_out_data(trained):
+    cl, _ = trained
+    r = cl.apriori(9001, 20)
+    # mean-square one-step error with the correction vs. without it (the plain solver)
+    assert r["apriori_mse_ratio"] < 0.6, r
+    assert r["apriori_gain"] > 1.3, r
+
+
+def test_corrected_run_is_finite_and_reported(trained):
+    cl, _ = trained
+    out = cl.evaluate(9001, 20)
+    print({k: out[k] for k in ("err_plain_lo", "err_closure_lo", "closure_gain",
+                               "speedup_closure_vs_hi", "err_hi_vs_fp64_hi")})
+    assert out["plain_lo_finite"] and out["closure_lo_finite"]
+    assert out["err_hi_vs_fp64_hi"] < 1e-5        # FP32 degree 10 vs FP64 degree 10
+    assert out["err_closure_lo"] < 0.5            # bounded (no blow-up) over 20 macro steps
+
+
+def test_fallback_to_degree_10_when_the_energy_check_fails(trained):
+    """The plain degree-10 solver is the fallback: a corrupted network (output layer scaled
+    by 1e4) makes the corrected run's energy grow, and solve() returns the degree-10 run."""
+    import torch
+    from bbdg.closure import project
+    cl, _ = trained
+    p0 = cl.net.params()
+    try:
+        p = p0.copy()
+        p[cl.nout_weight_slice()] *= 1e4
+        cl.net.set_params(p)
+        q, path, (e0, e1) = cl.solve(9002, 3)
+        assert path == "fallback", (e0, e1)
+        hi = cl.hi_solver()
+        q_hi = cl.initial_state(9002)
+        res = torch.zeros_like(q_hi)
+        hi.run(q_hi, res, cl.dt_hi, cl.cfg.hi_steps * 3)
+        want = project(q_hi, cl.cfg.N_hi, cl.cfg.N_lo)
+        torch.cuda.synchronize()
+        assert torch.equal(q, want)
+    finally:
+        cl.net.set_params(p0)
+    q, path, (e0, e1) = cl.solve(9002, 3)
+    assert bool(torch.isfinite(q).all())
+    assert (path == "closure") == (e1 <= e0 * 1.01), (path, e0, e1)

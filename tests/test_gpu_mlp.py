@@ -87,6 +87,51 @@ def test_gemm_epilogues(cuda):
     assert _rel(D.cpu(), want.cpu()) < 1e-5
 
 
+@pytest.mark.parametrize("N", [264, 203])
+def test_gemm_fixed_epilogues(cuda, N):
+    """The compile-time epilogues the MLP uses, with 16-byte row starts (N = 264) and without
+    (N = 203: scalar stores inside the same variant)."""
+    import torch
+    from bbdg import mlp
+    M, K = 520, 136
+    g = torch.Generator(device="cuda").manual_seed(N)
+    A = torch.randn((M, K), generator=g, device=cuda).bfloat16()
+    B = torch.randn((N, K), generator=g, device=cuda).bfloat16()
+    bias = torch.randn(N, generator=g, device=cuda)
+    z = A.double() @ B.double().T
+    # bias + GELU, pre-activation and BF16 output (the hidden layers' training forward)
+    pre = torch.empty((M, N), device=cuda)
+    Hb = torch.empty((M, N), device=cuda, dtype=torch.bfloat16)
+    HT = torch.empty((N, M), device=cuda, dtype=torch.bfloat16)
+    mlp.gemm_bf16(A, B, bias=bias, act=1, pre=pre, out_bf16=Hb, out_t=HT)
+    torch.cuda.synchronize()
+    zb = z + bias.double()
+    assert _rel(pre.cpu(), zb.cpu()) < 1e-5
+    want = torch.nn.functional.gelu(zb)
+    assert _rel(Hb.double().cpu(), want.cpu()) < 5e-3          # BF16 output
+    assert torch.equal(HT, Hb.T.contiguous())
+    # bias + FP32 output (the output layer)
+    C = torch.empty((M, N), device=cuda)
+    mlp.gemm_bf16(A, B, bias=bias, out_f32=C)
+    torch.cuda.synchronize()
+    assert _rel(C.cpu(), zb.cpu()) < 1e-5
+    # GELU' with BF16 output and bias gradient (the backward through a hidden layer)
+    D = torch.empty((M, N), device=cuda, dtype=torch.bfloat16)
+    bg = torch.zeros(N, device=cuda)
+    mlp.gemm_bf16(A, B, act=2, pre=pre, out_bf16=D, bias_grad=bg)
+    torch.cuda.synchronize()
+    p64 = pre.double()
+    dg = 0.5 * (1 + torch.erf(p64 / np.sqrt(2))) + p64 * torch.exp(-0.5 * p64 * p64) / np.sqrt(2 * np.pi)
+    want = z * dg
+    assert _rel(D.double().cpu(), want.cpu()) < 5e-3
+    assert _rel(bg.cpu(), want.sum(0).cpu()) < 1e-5
+    # BF16-only output
+    E = torch.empty((M, N), device=cuda, dtype=torch.bfloat16)
+    mlp.gemm_bf16(A, B, out_bf16=E)
+    torch.cuda.synchronize()
+    assert _rel(E.double().cpu(), z.cpu()) < 5e-3
+
+
 def test_gemm_rejects_bad_arguments(cuda):
     import torch
     from bbdg import mlp, BBError
