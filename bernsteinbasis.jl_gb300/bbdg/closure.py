@@ -93,6 +93,7 @@ class Closure:
         self.net.set_params(p)
         self.s_in = 1.0
         self.s_out = 1.0
+        self.weight = 1.0  # fraction of the network's correction applied per macro step
         self._X = torch.empty((self.K, self.nin), dtype=torch.bfloat16, device=self.device)
         self._Y = torch.empty((self.K, self.nout), dtype=torch.float32, device=self.device)
         self._res = self.lo.zeros()
@@ -122,13 +123,15 @@ class Closure:
         res.zero_()
         self.lo.run(q, res, self.dt_lo, self.lo_steps)
 
-    def correct(self, q: torch.Tensor, weight: float = 1.0) -> None:
-        """q += weight * MLP(features(q)) / s_out."""
+    def correct(self, q: torch.Tensor, weight: float | None = None) -> None:
+        """q += weight * MLP(features(q)) / s_out (weight: self.weight by default)."""
+        weight = self.weight if weight is None else weight
         closure_features(self.cfg.N_lo, NF, self.lo.conn, q, self.s_in, X=self._X)
         self.net.forward(self._X, out=self._Y)
         closure_apply(self.cfg.N_lo, NF, weight / self.s_out, self._Y, q)
 
-    def run_lo(self, q: torch.Tensor, nmacro: int, closure: bool, weight: float = 1.0) -> None:
+    def run_lo(self, q: torch.Tensor, nmacro: int, closure: bool,
+               weight: float | None = None) -> None:
         for _ in range(nmacro):
             self.plain_macro(q)
             if closure:
@@ -236,6 +239,28 @@ class Closure:
         return losses
 
     # ---- evaluation ----------------------------------------------------------------------
+    def select_weight(self, seed: int, nmacro: int, weights=(1.0, 0.5, 0.25)) -> dict:
+        """Model selection on a training initial condition: the correction weight whose
+        corrected run ends closest to the (FP32) degree-10 run; sets self.weight."""
+        hi = self.hi_solver()
+        q = self.initial_state(seed)
+        c0 = project(q, self.cfg.N_hi, self.cfg.N_lo)
+        res = torch.zeros_like(q)
+        hi.run(q, res, self.dt_hi, self.cfg.hi_steps * nmacro)
+        ref = project(q, self.cfg.N_hi, self.cfg.N_lo)
+        errs = {}
+        q5 = c0.clone()
+        self.run_lo(q5, nmacro, False)
+        errs["plain"] = self.rel_l2(q5, ref)
+        for w in weights:
+            q5 = c0.clone()
+            self.run_lo(q5, nmacro, True, float(w))
+            e = self.rel_l2(q5, ref)
+            errs[f"w{w:g}"] = e if math.isfinite(e) else float("inf")
+        best = min(weights, key=lambda w: errs[f"w{w:g}"])
+        self.weight = float(best)
+        return {"selected_weight": self.weight, "selection_errors": errs}
+
     def apriori(self, seed: int, nmacro: int) -> dict:
         """Teacher-forced one-macro-step error on one trajectory: sum over snapshots of
         |target - MLP| ^2 against |target|^2 (the plain solver's error), in scaled units."""
@@ -289,8 +314,8 @@ class Closure:
         out = {"seed": seed, "t_final": nmacro * self.macro, "hi_steps": self.cfg.hi_steps * nmacro,
                "lo_steps": self.lo_steps * nmacro, "hi_seconds": t_hi,
                "err_hi_vs_fp64_hi": err_hi_full, "err_hi_reduced": err_hi}
-        runs = [("plain", False, 1.0), ("closure", True, 1.0)]
-        runs += [(f"closure_w{w:g}", True, float(w)) for w in weights if w != 1.0]
+        runs = [("plain", False, 1.0), ("closure", True, self.weight)]
+        runs += [(f"closure_w{w:g}", True, float(w)) for w in weights if w != self.weight]
         for name, cl, w in runs:
             q5 = c0.clone()
             self.run_lo(q5.clone(), 1, cl, w)  # warm
@@ -324,10 +349,12 @@ class Closure:
 
     def save(self, path: str) -> None:
         np.savez(path, params=self.net.params(), s_in=self.s_in, s_out=self.s_out,
+                 weight=self.weight,
                  dims=np.array(self.net.dims), cfg=json.dumps(dataclasses.asdict(self.cfg)))
 
     def load(self, path: str) -> None:
         z = np.load(path)
         self.net.set_params(z["params"])
         self.s_in, self.s_out = float(z["s_in"]), float(z["s_out"])
+        self.weight = float(z["weight"]) if "weight" in z else 1.0
 

@@ -208,9 +208,12 @@ def config5(n: int = 16, n_train: int = 16, nmacro_train: int = 40, epochs: int 
                     log=lambda s: print(s, flush=True))
     info.update({"s_in": cl.s_in, "s_out": cl.s_out})
     print(json.dumps({"train": info}), flush=True)
+    sel = cl.select_weight(train_seeds[0], nmacro_eval)
+    print(json.dumps({"model_selection": sel}), flush=True)
     rows = []
     for s in eval_seeds:
         r = cl.evaluate(s, nmacro_eval, weights=(1.0, 0.5, 0.25))
+        r["weight"] = cl.weight
         r.update(cl.apriori(s, nmacro_eval))
         rows.append(r)
         print(json.dumps(r), flush=True)
