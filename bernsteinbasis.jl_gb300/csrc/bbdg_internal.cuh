@@ -102,6 +102,9 @@ int bb_fail(bb_ctx* ctx, int code, const char* fmt, ...);
 const DegTables* bb_tables(bb_ctx* ctx, int N);
 // The context's device error word (allocated on first use; nullptr on failure).
 int* bb_ctx_status_word(bb_ctx* ctx);
+// Degree-specialised FP32 lift (bbdg_lift_fast.cu): nfaces 4 or 1; -1 when N has none.
+int bb_lift_fast(bb_ctx* ctx, const DegTables* t, int64_t K, int nfaces, const void* x,
+                 void* out, cudaStream_t st);
 // Makes the context's device current.
 int bb_set_device(bb_ctx* ctx);
 // Checks a launch and counts it.

@@ -233,6 +233,78 @@ __global__ void __launch_bounds__(256) deriv_kernel(DegTables tab, const uint32_
   }
 }
 
+// Factored form of the same operators, D_a x(alpha) = 1/2 sum_b alpha_b w_a(alpha - e_b) with
+// w_a(beta) = x(beta + e_a) - x(beta + e_3) at degree N-1 (b over the four barycentric
+// indices; the reference's four terms per row, BernsteinDerivativeMatrix_3D.jl:96-216, are
+// exactly these). Per block: packed index tables in shared memory built once, then per tile
+// of EPB elements one pass forms w for every requested axis and one pass forms the outputs.
+template <class T>
+__global__ void __launch_bounds__(256) deriv_fact_kernel(DegTables tab,
+                                                         const uint32_t* __restrict__ gtab,
+                                                         int64_t K, int epb, int mask,
+                                                         const T* __restrict__ x,
+                                                         T* __restrict__ o0, T* __restrict__ o1,
+                                                         T* __restrict__ o2) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int N = tab.N, Np = tab.Np, NPM1 = tab.NpM1, NW = NPM1 + 1;
+  T* sx = reinterpret_cast<T*>(smem);                  // [epb][Np]
+  T* sW = sx + (size_t)epb * Np;                       // [3][epb][NW], entry NPM1 = 0
+  uint2* sVN = reinterpret_cast<uint2*>(smem + align16(sizeof(T) * ((size_t)epb * Np + 3 * (size_t)epb * NW)));
+  uint2* sGA = sVN + NPM1;                             // [Np] degree N-1 indices of alpha - e_b
+  uint32_t* sGW = reinterpret_cast<uint32_t*>(sGA + Np);  // [Np] alpha_b as 4 bytes
+  const uint32_t Z = (uint32_t)NPM1;
+  for (int t = threadIdx.x; t < NPM1; t += blockDim.x) {
+    const uint32_t c = gtab[tab.o_node3m1 + t];
+    const int i = c & 0xff, j = (c >> 8) & 0xff, k = c >> 16;
+    sVN[t] = make_uint2(ijk3(N, i + 1, j, k) | (ijk3(N, i, j + 1, k) << 16),
+                        ijk3(N, i, j, k + 1) | (ijk3(N, i, j, k) << 16));
+  }
+  for (int t = threadIdx.x; t < Np; t += blockDim.x) {
+    const uint32_t c = gtab[tab.o_node3 + t];
+    const int i = c & 0xff, j = (c >> 8) & 0xff, k = c >> 16, l = N - i - j - k;
+    const uint32_t m0 = i > 0 ? ijk3(N - 1, i - 1, j, k) : Z;
+    const uint32_t m1 = j > 0 ? ijk3(N - 1, i, j - 1, k) : Z;
+    const uint32_t m2 = k > 0 ? ijk3(N - 1, i, j, k - 1) : Z;
+    const uint32_t m3 = l > 0 ? ijk3(N - 1, i, j, k) : Z;
+    sGA[t] = make_uint2(m0 | (m1 << 16), m2 | (m3 << 16));
+    sGW[t] = (uint32_t)i | ((uint32_t)j << 8) | ((uint32_t)k << 16) | ((uint32_t)l << 24);
+  }
+  for (int t = threadIdx.x; t < 3 * epb; t += blockDim.x) sW[(size_t)t * NW + NPM1] = T(0);
+  T* outs[3] = {o0, o1, o2};
+  const int64_t nblk = (K + epb - 1) / epb;
+  for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+    const int64_t e0 = blk * epb;
+    const int ne = (int)min64(epb, K - e0);
+    __syncthreads();
+    copy_g2s(sx, x + e0 * Np, ne * Np);
+    __syncthreads();
+    for (int it = threadIdx.x; it < ne * NPM1; it += blockDim.x) {
+      const int le = it / NPM1, b = it - le * NPM1;
+      const uint2 vn = sVN[b];
+      const T* xe = sx + (size_t)le * Np;
+      const T x3 = xe[vn.y >> 16];
+      if (mask & 1) sW[((size_t)0 * epb + le) * NW + b] = xe[vn.x & 0xffff] - x3;
+      if (mask & 2) sW[((size_t)1 * epb + le) * NW + b] = xe[vn.x >> 16] - x3;
+      if (mask & 4) sW[((size_t)2 * epb + le) * NW + b] = xe[vn.y & 0xffff] - x3;
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < ne * Np; it += blockDim.x) {
+      const int le = it / Np, n = it - le * Np;
+      const uint2 ga = sGA[n];
+      const uint32_t gw = sGW[n];
+      const int m0 = ga.x & 0xffff, m1 = ga.x >> 16, m2 = ga.y & 0xffff, m3 = ga.y >> 16;
+      const T a0 = T(gw & 0xff), a1 = T((gw >> 8) & 0xff), a2 = T((gw >> 16) & 0xff),
+              a3 = T(gw >> 24);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        if (!(mask & (1 << a))) continue;
+        const T* w = sW + ((size_t)a * epb + le) * NW;
+        outs[a][e0 * Np + it] = T(0.5) * (a0 * w[m0] + a1 * w[m1] + a2 * w[m2] + a3 * w[m3]);
+      }
+    }
+  }
+}
+
 // -------------------------------------------------------------------------------------
 // lift kernels
 // -------------------------------------------------------------------------------------
@@ -372,6 +444,24 @@ static int grid_for(bb_ctx* ctx, int64_t nblk, int per_sm) {
 template <class T>
 static int launch_deriv(bb_ctx* ctx, const DegTables* t, int64_t K, int mask, const void* x,
                         void* o0, void* o1, void* o2, cudaStream_t st) {
+  {
+    // factored kernel: tile of epb elements plus the w rows and the index tables
+    int epb = 16;
+    size_t smem = 0;
+    for (; epb >= 1; epb /= 2) {
+      smem = align16(sizeof(T) * ((size_t)epb * t->Np + 3 * (size_t)epb * (t->NpM1 + 1))) +
+             8 * (size_t)t->NpM1 + 8 * (size_t)t->Np + 4 * (size_t)t->Np;
+      if (smem <= 48 * 1024) break;
+    }
+    if (epb >= 1 && t->Np <= 65535) {
+      BB_CUDA(ctx, cudaFuncSetAttribute(deriv_fact_kernel<T>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      const int64_t nblk = (K + epb - 1) / epb;
+      deriv_fact_kernel<T><<<grid_for(ctx, nblk, 8), 256, smem, st>>>(
+          *t, t->d_words, K, epb, mask, (const T*)x, (T*)o0, (T*)o1, (T*)o2);
+      return bb_check_launch(ctx, "deriv_fact_kernel");
+    }
+  }
   const int epb = 8;
   const size_t smem = align16(sizeof(T) * (size_t)epb * t->Np) + 4 * (size_t)t->nwords;
   if (smem > ctx->smem_optin) return bb_fail(ctx, BB_ERR_ARG, "degree too large for deriv tile");
@@ -386,6 +476,10 @@ static int launch_deriv(bb_ctx* ctx, const DegTables* t, int64_t K, int mask, co
 template <class T>
 static int launch_lift(bb_ctx* ctx, const DegTables* t, int64_t K, int nfaces, const void* x,
                        void* out, cudaStream_t st) {
+  if (sizeof(T) == 4) {
+    const int rc = bb_lift_fast(ctx, t, K, nfaces, x, out, st);
+    if (rc >= 0) return rc;  // otherwise no specialised kernel for this degree
+  }
   const int S = np2(t->N + 1);
   int epb = 8;
   size_t smem = 0;

@@ -21,9 +21,12 @@
 //
 // Block organisation: EPB elements per tile; TPE "element threads" per element plus
 // CHT "chain threads" (whole warps, one lift chain each). Tiles stream through a persistent
-// loop: q, geometry and connectivity of the next tile and res of the current one arrive by
-// bulk copies (cp.async.bulk, mbarrier completion, bounded waits); q and res leave by bulk
-// stores.
+// loop in two phases: (A) the chain warp lifts tile i while the element threads form the
+// volume term of tile i and the interface flux of tile i+1 (double-buffered chain inputs);
+// (B) the element threads gather the lift stacks, add the volume term and apply the LSRK
+// update, storing q, res and the outgoing face traces straight to HBM. q, geometry and
+// connectivity of tile i+2 and res of tile i+1 arrive by bulk copies (cp.async.bulk,
+// mbarrier completion, bounded waits) while tiles i and i+1 are being worked on.
 #include <cmath>
 
 #include "bbdg_internal.cuh"
@@ -86,9 +89,11 @@ struct FastLayout {
   static constexpr int FVOL_B = VN_B + NPM1 * 8;               // [4][NFP] u16
   static constexpr int FPERM_B = FVOL_B + ((4 * NFP * 2 + 3) / 4 * 4);  // [6][NFP] u16
   static constexpr int FNB_B = FPERM_B + ((6 * NFP * 2 + 3) / 4 * 4);  // [4][6][NFP] u16
-  static constexpr int BAR_B = (FNB_B + 24 * NFP * 2 + 15) / 16 * 16;  // 3 mbarriers
+  static constexpr int TF_B = (FNB_B + 24 * NFP * 2 + 15) / 16 * 16;   // [NP] u32 face nodes
+  static constexpr int BAR_B = (TF_B + NP * 4 + 15) / 16 * 16;         // 3 mbarriers
   static constexpr int BYTES = BAR_B + 32;
   static_assert((EPB * NP * 4) % 16 == 0, "tile segments must be multiples of 16 bytes");
+  static_assert(NFP < 255, "face node indices are packed in bytes");
   static_assert(TPE % 32 == 0 && TPE >= 32, "element threads come in whole warps");
 };
 
@@ -131,6 +136,10 @@ __device__ __forceinline__ void tma_load(void* dst, const void* src, uint32_t by
       "l"(src), "r"(bytes), "r"(s_addr(bar))
       : "memory");
 }
+// Asks the memory system to bring [src, src + bytes) into L2 (no completion to wait for).
+__device__ __forceinline__ void l2_prefetch(const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void tma_store(void* dst, const void* src, uint32_t bytes) {
   asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst),
                "r"(s_addr(src)), "r"(bytes)
@@ -149,9 +158,9 @@ __device__ __forceinline__ void named_sync(int id, int count) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
 
-// One face lift chain for compile-time N: x = chain input (NFP values, smem, may alias the
-// tail of g); g = the face's volume stack, g[c_ijk(N,i,j,d)] = E_d(i,j) (unscaled; the
-// l_d factors are applied when the stacks are summed). All of x is read before g is written.
+// One face lift chain for compile-time N: x = chain input (NFP values, smem); g = the face's
+// volume stack, g[c_ijk(N,i,j,d)] = E_d(i,j) (unscaled; the l_d factors are applied when the
+// stacks are summed). All of x is read before g is written.
 template <int N>
 __device__ __forceinline__ void lift_chain(const float* x, float* g) {
   constexpr int NFP = (N + 1) * (N + 2) / 2;
@@ -220,6 +229,8 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT, 2)
   uint16_t* sFperm = reinterpret_cast<uint16_t*>(smem + L::FPERM_B);
   // partner face nf, orientation o, node a -> volume index of the partner's node
   uint16_t* sFnb = reinterpret_cast<uint16_t*>(smem + L::FNB_B);
+  // per coefficient: its node index on faces f0..f3 (one byte each, 0xff = not on the face)
+  uint32_t* sTF = reinterpret_cast<uint32_t*>(smem + L::TF_B);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L::BAR_B);  // [0],[1] q slots, [2] res
   __shared__ int s_fail;
   const int tid = threadIdx.x;
@@ -284,6 +295,12 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT, 2)
       // layer 0 carries the L0 block itself (weight 1)
       auto lw = [](int d) { return d == 0 ? 1.0f : lift_lj(N, d); };
       sLW[t] = make_float4(lw(j), lw(l), lw(i), lw(k));
+      // face nodes: f0 (j=0) at (i,k), f1 (l=0) at (j,k), f2 (i=0) at (j,k), f3 (k=0) at (i,j)
+      const uint32_t a0 = j == 0 ? (uint32_t)ij2(N, i, k) : 0xffu;
+      const uint32_t a1 = l == 0 ? (uint32_t)ij2(N, j, k) : 0xffu;
+      const uint32_t a2 = i == 0 ? (uint32_t)ij2(N, j, k) : 0xffu;
+      const uint32_t a3 = k == 0 ? (uint32_t)ij2(N, i, j) : 0xffu;
+      sTF[t] = a0 | (a1 << 8) | (a2 << 16) | (a3 << 24);
     }
     for (int t = tid; t < NPM1; t += NT) {
       const uint32_t c = gw[P.o_node3m1 + t];
@@ -411,6 +428,12 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT, 2)
       const int c = tid - NTE;
       if (c < NCHAIN) lift_chain<N>(sX + (s * NCHAIN + c) * NFP, sG + c * NPS);
     } else {
+      // the tile after next: its outside-tile neighbour traces (one contiguous NF x Nfp block
+      // per face) are pulled into L2 now, a whole tile ahead of its flux phase
+      const int64_t tpre = tnext + gridDim.x;
+      int32_t cpre = 0;
+      const bool pre = fa0 == 0 && tpre < ntiles && P.trace_in != nullptr;
+      if (pre) cpre = __ldg(gconn + (tpre * EPB + le) * 4 + ff);
       const float* g = sGeo + le * BB_GEO_STRIDE;
       // barycentric weights of J d/dx, J d/dy, J d/dz: g_a = (rxJ, sxJ, txJ, -sum)/2; the
       // sum over a is formed as sum_{a<3} g_a (x_a - x_3), which cancels smooth data
@@ -463,6 +486,12 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT, 2)
 #pragma unroll
         for (int m = 0; m < NW; ++m) sW[(m * EPB + le) * L::NPM1P + b] = w[m];
       }
+      if (pre) {
+        const int64_t nb = (int64_t)((uint32_t)cpre >> 5);
+        const int nfc = (cpre >> 3) & 3;
+        if (nb < K && (nb < tpre * EPB || nb >= (tpre + 1) * EPB))
+          l2_prefetch(P.trace_in + ((size_t)nb * 4 + nfc) * NF * NFP, NF * NFP * 4);
+      }
       if (tnext < ntiles) {
         if (!mbar_wait(&bar[s ^ 1], (ph >> (s ^ 1)) & 1u)) s_fail = 1;
         ph ^= 1u << (s ^ 1);
@@ -489,6 +518,16 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT, 2)
       }
       const float* G = sG + le * 4 * NCH * NPS;
       const float* wb = sW + le * L::NPM1P;
+      // faces whose partner lies outside this tile need their updated trace in HBM
+      bool leave[4];
+#pragma unroll
+      for (int f = 0; f < 4; ++f) {
+        const int64_t nb = (int64_t)((uint32_t)sConn[le * 4 + f] >> 5);
+        leave[f] = P.trace_out != nullptr && (nb < e0 || nb >= e0 + EPB);
+      }
+      // all right-hand sides of this thread first (shared-memory reads only), then the
+      // updates and stores, so that no store sits between the loads of different r
+      float rhs_all[GR][NF];
 #pragma unroll
       for (int r = 0; r < GR; ++r) {
         const int n = u + r * TPE;
@@ -505,7 +544,7 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT, 2)
           const float* wm = wb + m * EPB * L::NPM1P;
           vol[m] = fmaf(gw4.x, wm[x0], fmaf(gw4.y, wm[x1], fmaf(gw4.z, wm[x2], gw4.w * wm[x3])));
         }
-        float rhs[NF];
+        float* rhs = rhs_all[r];
         if constexpr (PHYS == BB_WAVE) {
           // face order of src/BernsteinLift.jl:202-214: t=-1 face first, then f1, f2, f3
           const float B3 = lwf[3] * G[(3 * 2 + 1) * NPS + p[3]];
@@ -532,58 +571,52 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT, 2)
             rhs[m] = (v + vol[m]) * invJ;
           }
         }
+      }
+      float* __restrict__ gq_out = P.q;
+      float* __restrict__ gres_out = P.res;
+      float* __restrict__ grhs_out = P.rhs;
+#pragma unroll
+      for (int r = 0; r < GR; ++r) {
+        const int n = u + r * TPE;
+        if (n >= NP) continue;
+        const float* rhs = rhs_all[r];
         const int item = le * NP + n;
         if (!stage) {
 #pragma unroll
-          for (int m = 0; m < NF; ++m) P.rhs[((size_t)m * K + e0) * NP + item] = rhs[m];
+          for (int m = 0; m < NF; ++m) grhs_out[((size_t)m * K + e0) * NP + item] = rhs[m];
         } else {
+          // q and res leave straight from registers (coalesced: item runs along the tile),
+          // and so do the outgoing face traces of the coefficients that lie on a face
+          float qn[NF];
 #pragma unroll
           for (int m = 0; m < NF; ++m) {
             const float rr = fmaf(rkA, sRes[m * EPB * NP + item], dt * rhs[m]);
-            sRes[m * EPB * NP + item] = rr;
-            sQ[m * EPB * NP + item] = fmaf(rkB, rr, sQ[m * EPB * NP + item]);
+            qn[m] = fmaf(rkB, rr, sQ[m * EPB * NP + item]);
+            gres_out[((size_t)m * K + e0) * NP + item] = rr;
+            gq_out[((size_t)m * K + e0) * NP + item] = qn[m];
+          }
+          const uint32_t tf = sTF[n];
+#pragma unroll
+          for (int f = 0; f < 4; ++f) {
+            const uint32_t a = (tf >> (8 * f)) & 0xffu;
+            if (a != 0xffu && leave[f]) {
+              float* dst = P.trace_out + ((size_t)(e0 + le) * 4 + f) * NF * NFP + a;
+#pragma unroll
+              for (int m = 0; m < NF; ++m) dst[m * NFP] = qn[m];
+            }
           }
         }
       }
     }
     __syncthreads();
-
-    // ---- C. write back q and res (bulk stores) and the outgoing traces ----------------
-    if (stage) {
-      if (tid == 0) {
-        fence_async_smem();  // make the generic-proxy smem writes visible to the bulk copies
-#pragma unroll
-        for (int m = 0; m < NF; ++m) {
-          tma_store(P.q + ((size_t)m * K + e0) * NP, sQ + m * EPB * NP, EPB * NP * 4);
-          tma_store(P.res + ((size_t)m * K + e0) * NP, sRes + m * EPB * NP, EPB * NP * 4);
-        }
-        tma_store_commit();
-      }
-      if (P.trace_out && is_elem) {
-        const int64_t nbr = (int64_t)((uint32_t)sConn[le * 4 + ff] >> 5);
-        if (nbr < e0 || nbr >= e0 + EPB) {
-          float* dst0 = P.trace_out + ((size_t)(e0 + le) * 4 + ff) * NF * NFP;
-#pragma unroll
-          for (int r = 0; r < FR; ++r) {
-            const int a = fa0 + r * FT;
-            if (a >= NFP) continue;
-            const float* src = sQ + le * NP + sFvol[ff * NFP + a];
-#pragma unroll
-            for (int m = 0; m < NF; ++m) dst0[m * NFP + a] = src[m * EPB * NP];
-          }
-        }
-      }
-    }
-    __syncthreads();
-    // refill: this slot takes the tile after next, the res buffer the next tile
+    // the slot and the res buffer are free: fetch the tile after next into this slot and the
+    // next tile's res, both well ahead of their use
     if (tid == 0) {
       const int64_t tnn = tnext + gridDim.x;
-      const bool more_q = tnn < ntiles, more_res = stage && tnext < ntiles;
-      if (more_q || more_res) {
-        tma_store_wait_read();  // the bulk stores have read this slot and the res buffer
-        fence_async_smem();
-        if (more_q) issue_main(tnn, s);
-        if (more_res) issue_res(tnext);
+      if (tnn < ntiles || (stage && tnext < ntiles)) {
+        fence_async_smem();  // order the generic-proxy reads before the copies
+        if (tnn < ntiles) issue_main(tnn, s);
+        if (stage && tnext < ntiles) issue_res(tnext);
       }
     }
   }

@@ -95,8 +95,11 @@ def test_fused_operator_pass(cuda, bb, N):
     ref = [torch.empty_like(x) for _ in range(4)]
     bb.grad_(ref[0], ref[1], ref[2], N, x)
     bb.mul_(ref[3], bb.BernsteinLift(N), f)
-    for a, b in zip((dr, ds, dt_, li), ref):
-        assert torch.equal(a, b)
+    # the separate derivative calls use the factored form (w at degree N-1), the fused pass
+    # the reference's per-row form: equal up to rounding; the lift is the same kernel
+    for a, b in zip((dr, ds, dt_), ref[:3]):
+        assert rel(a.cpu().numpy(), b.cpu().numpy()) < 1e-14
+    assert torch.equal(li, ref[3])
 
 
 def _golden():
