@@ -20,8 +20,8 @@ from .context import dtype_code, get_context, stream_handle
 from .mesh import uniform_tet_mesh
 from .ordering import np3
 
-PHYS_CODE = {"wave": _lib.BB_WAVE, "maxwell": _lib.BB_MAXWELL}
-NFIELDS = {"wave": 4, "maxwell": 6}
+PHYS_CODE = {"wave": _lib.BB_WAVE, "maxwell": _lib.BB_MAXWELL, "advection": _lib.BB_ADVECTION}
+NFIELDS = {"wave": 4, "maxwell": 6, "advection": 1}
 
 
 @dataclass
@@ -46,11 +46,12 @@ def config4_problems(seed: int = 2, count: int = 48):
 
 
 def initial_state(spec: ProblemSpec, mesh) -> np.ndarray:
-    """Gaussian-pulse sum in p (wave) or E_z (Maxwell), the other fields zero (FP64)."""
+    """Gaussian-pulse sum in p (wave), E_z (Maxwell) or u (advection), the other fields zero
+    (FP64)."""
     zero = lambda x, y, z: 0 * x  # noqa: E731
     f = gaussian_pulses(spec.seed)
     nf = NFIELDS[spec.physics]
-    fields = [f] + [zero] * 3 if spec.physics == "wave" else [zero] * 5 + [f]
+    fields = {"wave": [f] + [zero] * 3, "maxwell": [zero] * 5 + [f], "advection": [f]}[spec.physics]
     assert len(fields) == nf
     return project_fields(mesh, spec.N, fields)
 

@@ -1,11 +1,13 @@
-"""DG solvers for the wave and Maxwell examples on the GPU.
+"""DG solvers for the wave, Maxwell and scalar advection examples on the GPU.
 
 Replaces the examples' ``rhs_matvec!`` + ``solve(ODEProblem(...), Tsit5())`` loop
-(examples/3d_wave.jl:36-84,:133-134; examples/3d_maxwell.jl:36-93,:137-138) with a fused
-RHS + 5-stage low-storage RK kernel per stage, replayed from a CUDA graph per step.
+(examples/3d_wave.jl:36-84,:133-134; examples/3d_maxwell.jl:36-93,:137-138;
+examples/3d_advec_scalar.jl:17-42,:84-85) with a fused RHS + 5-stage low-storage RK kernel
+per stage, replayed from a CUDA graph per step.
 
 State layout: a (nf, K, Np) CUDA tensor; field m is the reference's Np x K matrix of that
-component (p, u, v, w for the wave equation; Hx, Hy, Hz, Ex, Ey, Ez for Maxwell).
+component (p, u, v, w for the wave equation; Hx, Hy, Hz, Ex, Ey, Ez for Maxwell; u for
+advection).
 """
 from __future__ import annotations
 
@@ -20,7 +22,8 @@ from .context import dtype_code, get_context, ptr, require_cuda, stream_handle
 from .mesh import TetMesh
 from .ordering import np3
 
-PHYSICS = {"wave": (_lib.BB_WAVE, 4), "maxwell": (_lib.BB_MAXWELL, 6)}
+PHYSICS = {"wave": (_lib.BB_WAVE, 4), "maxwell": (_lib.BB_MAXWELL, 6),
+           "advection": (_lib.BB_ADVECTION, 1)}
 
 
 class DGSolver:

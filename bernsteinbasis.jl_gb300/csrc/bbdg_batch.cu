@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(kBatchThreads, 3)
           sP.trace_out = d.trace[par ^ 1];
           s_phys = d.physics;
           s_begin = d.tile_begin;
-          const int NF = d.physics == BB_WAVE ? 4 : 6;
+          const int NF = physics_nf(d.physics);
           sL = tile_layout_for(d.P.tab.N, NF, NF, sizeof(T), d.P.tab.nwords, d.P.epb);
           s_prob = p;
           s_reload = 1;
@@ -80,8 +80,10 @@ __global__ void __launch_bounds__(kBatchThreads, 3)
     const SmemTables st = tables_view(sP.tab, stab);
     if (s_phys == BB_WAVE)
       generic_stage_tile<T, BB_WAVE>(sP, sL, st, item - s_begin);  // starts with a barrier
-    else
+    else if (s_phys == BB_MAXWELL)
       generic_stage_tile<T, BB_MAXWELL>(sP, sL, st, item - s_begin);
+    else
+      generic_stage_tile<T, BB_ADVECTION>(sP, sL, st, item - s_begin);
   }
 }
 
@@ -172,7 +174,7 @@ int build_desc(bb_batch* b) {
     d.tile_begin = begin;
     d.physics = pr.physics;
     begin += (pr.K + b->epb[p] - 1) / b->epb[p];
-    const int nf = pr.physics == BB_WAVE ? 4 : 6;
+    const int nf = physics_nf(pr.physics);
     const TileLayout L = tile_layout_for(pr.N, nf, nf, sizeof(T), t->nwords, b->epb[p]);
     smem = std::max(smem, L.total);
   }
@@ -212,11 +214,14 @@ int batch_extract(bb_batch* b, cudaStream_t st) {
   for (size_t p = 0; p < b->probs.size(); ++p) {
     const bb_batch_problem& pr = b->probs[p];
     const DegTables& t = *b->tabs[p];
-    const int nf = pr.physics == BB_WAVE ? 4 : 6;
+    const int nf = physics_nf(pr.physics);
     int64_t grid = (pr.K * 4 * nf * t.Nfp + 255) / 256;
     grid = std::min<int64_t>(std::max<int64_t>(grid, 1), (int64_t)b->ctx->num_sms * 8);
     if (nf == 4)
       batch_extract_kernel<T, 4><<<(int)grid, 256, 0, st>>>(t, t.d_words, pr.K, (const T*)pr.q,
+                                                            (T*)b->trace[2 * p]);
+    else if (nf == 1)
+      batch_extract_kernel<T, 1><<<(int)grid, 256, 0, st>>>(t, t.d_words, pr.K, (const T*)pr.q,
                                                             (T*)b->trace[2 * p]);
     else
       batch_extract_kernel<T, 6><<<(int)grid, 256, 0, st>>>(t, t.d_words, pr.K, (const T*)pr.q,
@@ -292,7 +297,7 @@ extern "C" int bb_batch_create(bb_ctx* ctx, int nprob, const bb_batch_problem* p
   b->dtype = dtype;
   for (int p = 0; p < nprob; ++p) {
     const bb_batch_problem& pr = probs[p];
-    if ((pr.physics != BB_WAVE && pr.physics != BB_MAXWELL) || !valid_degree(pr.N) || pr.K < 1 ||
+    if (physics_nf(pr.physics) == 0 || !valid_degree(pr.N) || pr.K < 1 ||
         pr.K >= (int64_t(1) << 27) || !pr.conn || !pr.geo || !pr.q || !pr.res ||
         !std::isfinite(pr.dt) || !std::isfinite(pr.tau)) {
       free_batch(b);
@@ -305,7 +310,7 @@ extern "C" int bb_batch_create(bb_ctx* ctx, int nprob, const bb_batch_problem* p
     }
     b->probs.push_back(pr);
     b->tabs.push_back(t);
-    const int nf = pr.physics == BB_WAVE ? 4 : 6;
+    const int nf = physics_nf(pr.physics);
     b->epb.push_back(batch_tile_default(pr.N, nf, dtype));
     const size_t bytes = (size_t)pr.K * 4 * nf * t->Nfp * dtype_size(dtype);
     for (int k = 0; k < 2; ++k) {
@@ -339,7 +344,7 @@ extern "C" int bb_batch_set_tile(bb_batch* b, int physics, int N, int elems_per_
   if (!b) return BB_ERR_ARG;
   if (elems_per_block < 1 || elems_per_block > 64)
     return bb_fail(b->ctx, BB_ERR_ARG, "elements per block must be 1..64");
-  const int nf = physics == BB_WAVE ? 4 : 6;
+  const int nf = physics_nf(physics);
   const TileLayout L = tile_layout_for(N, nf, nf, dtype_size(b->dtype), 1 << 12, elems_per_block);
   if (L.total > b->ctx->smem_optin)
     return bb_fail(b->ctx, BB_ERR_ARG, "tile of %d elements exceeds shared memory", elems_per_block);

@@ -111,6 +111,10 @@ int bb_set_device(bb_ctx* ctx);
 int bb_check_launch(bb_ctx* ctx, const char* what);
 
 inline size_t dtype_size(int dtype) { return dtype == BB_F64 ? 8 : 4; }
+// Fields of a physics code, 0 if unknown.
+__host__ __device__ inline int physics_nf(int physics) {
+  return physics == BB_WAVE ? 4 : physics == BB_MAXWELL ? 6 : physics == BB_ADVECTION ? 1 : 0;
+}
 inline bool valid_dtype(int dtype) { return dtype == BB_F32 || dtype == BB_F64; }
 inline bool valid_degree(int N) { return N >= 1 && N <= BB_MAX_DEGREE; }
 

@@ -89,6 +89,9 @@ int solver_layout(bb_solver* s, int epb, size_t* smem_out) {
   if (s->physics == BB_WAVE)
     L = s->dtype == BB_F64 ? tile_layout<double, BB_WAVE>(*s->tab, epb)
                            : tile_layout<float, BB_WAVE>(*s->tab, epb);
+  else if (s->physics == BB_ADVECTION)
+    L = s->dtype == BB_F64 ? tile_layout<double, BB_ADVECTION>(*s->tab, epb)
+                           : tile_layout<float, BB_ADVECTION>(*s->tab, epb);
   else
     L = s->dtype == BB_F64 ? tile_layout<double, BB_MAXWELL>(*s->tab, epb)
                            : tile_layout<float, BB_MAXWELL>(*s->tab, epb);
@@ -177,6 +180,10 @@ int launch_stage(bb_solver* s, int mode, int stage, double dt, void* q, void* re
     return s->dtype == BB_F64
                ? launch_stage_t<double, BB_WAVE>(s, mode, stage, dt, q, res, rhs, tin, tout, st)
                : launch_stage_t<float, BB_WAVE>(s, mode, stage, dt, q, res, rhs, tin, tout, st);
+  if (s->physics == BB_ADVECTION)
+    return s->dtype == BB_F64
+               ? launch_stage_t<double, BB_ADVECTION>(s, mode, stage, dt, q, res, rhs, tin, tout, st)
+               : launch_stage_t<float, BB_ADVECTION>(s, mode, stage, dt, q, res, rhs, tin, tout, st);
   return s->dtype == BB_F64
              ? launch_stage_t<double, BB_MAXWELL>(s, mode, stage, dt, q, res, rhs, tin, tout, st)
              : launch_stage_t<float, BB_MAXWELL>(s, mode, stage, dt, q, res, rhs, tin, tout, st);
@@ -191,11 +198,15 @@ int launch_extract(bb_solver* s, const void* q, void* tr, cudaStream_t st) {
   if (s->dtype == BB_F64) {
     if (s->nf == 4)
       extract_traces_kernel<double, 4><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr);
+    else if (s->nf == 1)
+      extract_traces_kernel<double, 1><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr);
     else
       extract_traces_kernel<double, 6><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr);
   } else {
     if (s->nf == 4)
       extract_traces_kernel<float, 4><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr);
+    else if (s->nf == 1)
+      extract_traces_kernel<float, 1><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr);
     else
       extract_traces_kernel<float, 6><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr);
   }
@@ -255,8 +266,8 @@ extern "C" int bb_solver_create(bb_ctx* ctx, int physics, int N, int64_t K, int 
                                 bb_solver** out) {
   if (!ctx || !out) return BB_ERR_ARG;
   *out = nullptr;
-  if (physics != BB_WAVE && physics != BB_MAXWELL)
-    return bb_fail(ctx, BB_ERR_ARG, "physics must be BB_WAVE or BB_MAXWELL");
+  if (physics_nf(physics) == 0)
+    return bb_fail(ctx, BB_ERR_ARG, "physics must be BB_WAVE, BB_MAXWELL or BB_ADVECTION");
   if (!valid_degree(N)) return bb_fail(ctx, BB_ERR_ARG, "degree N=%d outside 1..%d", N, BB_MAX_DEGREE);
   if (!valid_dtype(dtype)) return bb_fail(ctx, BB_ERR_ARG, "bad dtype");
   if (K < 1 || K >= (int64_t(1) << 27)) return bb_fail(ctx, BB_ERR_ARG, "K must be in 1..2^27-1");
@@ -273,7 +284,7 @@ extern "C" int bb_solver_create(bb_ctx* ctx, int physics, int N, int64_t K, int 
   s->N = N;
   s->K = K;
   s->dtype = dtype;
-  s->nf = physics == BB_WAVE ? 4 : 6;
+  s->nf = physics_nf(physics);
   s->conn = conn;
   s->geo = geo;
   s->tau = tau;

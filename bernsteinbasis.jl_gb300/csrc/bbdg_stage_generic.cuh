@@ -32,6 +32,14 @@ struct Phys<BB_MAXWELL> {
   static constexpr int NW = 6;  // curl terms
   static constexpr float vol_sign = 1.f;
 };
+// examples/3d_advec_scalar.jl: du = -(LIFT flux + J du/dx) / J; the flux is stored negated
+// so that the shared "sign * volume + lift" combination gives the example's right-hand side.
+template <>
+struct Phys<BB_ADVECTION> {
+  static constexpr int NF = 1;  // u
+  static constexpr int NW = 1;  // J du/dx
+  static constexpr float vol_sign = -1.f;
+};
 
 template <class T>
 struct StageParams {
@@ -157,7 +165,11 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
         cu = P.tau / Jf;
       }
       T fl[NF];
-      if constexpr (PHYS == BB_WAVE) {
+      if constexpr (PHYS == BB_ADVECTION) {
+        // 3d_advec_scalar.jl:24-29: 0.5 du nxJ - 0.5 du Jf (negated, see Phys<BB_ADVECTION>)
+        const T Jf = sqrt(nx * nx + ny * ny + nz * nz);
+        fl[0] = -(T(0.5) * d[0] * nx - T(0.5) * d[0] * Jf);
+      } else if constexpr (PHYS == BB_WAVE) {
         // 3d_wave.jl:45-54
         const T ndotdU = nx * d[1] + ny * d[2] + nz * d[3];
         const T A = cp * d[0] - ndotdU;
@@ -206,7 +218,11 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
       for (int m = 0; m < NW; ++m) w[m] = T(0);
       // sum_a g_a x(beta+e_a) with sum_a g_a = 0, formed as sum_{a<3} g_a (x_a - x_3) so
       // that smooth data cancels in the differences (as the reference's Dr = (D0 - D3)/2)
-      if constexpr (PHYS == BB_WAVE) {
+      if constexpr (PHYS == BB_ADVECTION) {
+        const T u3 = F(0, 3);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) w[0] += gx[a] * (F(0, a) - u3);  // J du/dx
+      } else if constexpr (PHYS == BB_WAVE) {
         const T p3 = F(0, 3), u3 = F(1, 3), v3 = F(2, 3), w3 = F(3, 3);
 #pragma unroll
         for (int a = 0; a < 3; ++a) {

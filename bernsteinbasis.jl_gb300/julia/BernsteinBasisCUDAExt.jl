@@ -24,6 +24,7 @@ const BB_F32 = Cint(0)
 const BB_F64 = Cint(1)
 const BB_WAVE = Cint(0)
 const BB_MAXWELL = Cint(1)
+const BB_ADVECTION = Cint(2)   # examples/3d_advec_scalar.jl
 
 dtype_code(::Type{Float32}) = BB_F32
 dtype_code(::Type{Float64}) = BB_F64
@@ -94,13 +95,14 @@ end
 function BBSolver(physics::Symbol, N::Integer, conn::CuVector{Int32}, geo::CuVector{T};
                   tau::Real = 1.0) where {T<:Union{Float32,Float64}}
     code = physics === :wave ? BB_WAVE : physics === :maxwell ? BB_MAXWELL :
-           throw(ArgumentError("physics must be :wave or :maxwell"))
+           physics === :advection ? BB_ADVECTION :
+           throw(ArgumentError("physics must be :wave, :maxwell or :advection"))
     r = Ref{Ptr{Cvoid}}(C_NULL)
     K = length(conn) ÷ 4
     check(ccall((:bb_solver_create, libbbdg), Cint,
                 (Ptr{Cvoid}, Cint, Cint, Int64, Cint, CuPtr{Int32}, CuPtr{T}, Cdouble, Ptr{Ptr{Cvoid}}),
                 context(), code, N, K, dtype_code(T), conn, geo, tau, r))
-    s = BBSolver{T}(r[], physics === :wave ? 4 : 6, conn, geo)
+    s = BBSolver{T}(r[], physics === :wave ? 4 : physics === :maxwell ? 6 : 1, conn, geo)
     finalizer(s -> ccall((:bb_solver_destroy, libbbdg), Cint, (Ptr{Cvoid},), s.handle), s)
     return s
 end

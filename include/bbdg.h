@@ -40,7 +40,10 @@ typedef enum {
 } bb_status;
 
 typedef enum { BB_F32 = 0, BB_F64 = 1 } bb_dtype;
-typedef enum { BB_WAVE = 0, BB_MAXWELL = 1 } bb_physics;
+/* BB_WAVE: examples/3d_wave.jl (p, u, v, w); BB_MAXWELL: examples/3d_maxwell.jl
+ * (Hx, Hy, Hz, Ex, Ey, Ez); BB_ADVECTION: examples/3d_advec_scalar.jl (u, du/dt + du/dx = 0,
+ * upwind flux with the face Jacobian; tau does not enter, the generic kernel runs it). */
+typedef enum { BB_WAVE = 0, BB_MAXWELL = 1, BB_ADVECTION = 2 } bb_physics;
 typedef enum { BB_AXIS_R = 0, BB_AXIS_S = 1, BB_AXIS_T = 2 } bb_axis;
 
 #define BB_MAX_DEGREE 20
@@ -148,7 +151,7 @@ int bb_project(bb_ctx* ctx, int N, int M, int64_t K, int nf, int dtype_in, const
  * examples/3d_maxwell.jl). Arrays are device pointers in the batch dtype and must outlive
  * the batch object. */
 typedef struct {
-  int physics;          /* BB_WAVE or BB_MAXWELL */
+  int physics;          /* BB_WAVE, BB_MAXWELL or BB_ADVECTION */
   int N;                /* degree, 1..BB_MAX_DEGREE */
   int64_t K;            /* elements */
   const int32_t* conn;  /* K*4 packed connectivity (as bb_solver_create) */

@@ -352,7 +352,14 @@ void rhs_example(int N, int K, const SV<T, NF>* q, SV<T, NF>* du, const int* Fma
         cu = tau / Jf;
       }
       V fl;
-      if constexpr (NF == 4) {
+      if constexpr (NF == 1) {
+        // examples/3d_advec_scalar.jl:24-29: upwind flux of du/dt + du/dx = 0 with the face
+        // Jacobian Jf = |nJ| (written with Jf as the examples do; tau does not enter)
+        const T Jf = std::sqrt(nx * nx + ny * ny + nz * nz);
+        (void)cp;
+        (void)cu;
+        fl.v[0] = T(0.5) * duM.v[0] * nx - T(0.5) * duM.v[0] * Jf;
+      } else if constexpr (NF == 4) {
         const T ndotdU = nx * duM.v[1] + ny * duM.v[2] + nz * duM.v[3];
         const T a = cp * duM.v[0] - ndotdU;
         const T b = cu * ndotdU - duM.v[0];
@@ -389,10 +396,15 @@ void rhs_example(int N, int K, const SV<T, NF>* q, SV<T, NF>* du, const int* Fma
     for (int e = 0; e < K; ++e) {
       const V* qe = q + (size_t)e * Np;
       for (int n = 0; n < Np; ++n) {
-        if constexpr (NF == 4)
+        if constexpr (NF == 1) {
+          fxu[n] = qe[n];  // fx(u) = u, fy = fz = 0 (3d_advec_scalar.jl:33-35)
+          fyu[n] = V{};
+          fzu[n] = V{};
+        } else if constexpr (NF == 4) {
           wave_fluxes(qe[n], fxu[n], fyu[n], fzu[n]);
-        else
+        } else {
           maxwell_fluxes(qe[n], fxu[n], fyu[n], fzu[n]);
+        }
       }
       fast_Dr(d[0].data(), N, fxu.data(), o);
       fast_Ds(d[1].data(), N, fxu.data(), o);
@@ -414,8 +426,10 @@ void rhs_example(int N, int K, const SV<T, NF>* q, SV<T, NF>* du, const int* Fma
         if constexpr (NF == 4)
           due[i] = due[i] - vol;  // wave: du -= ... (3d_wave.jl:76)
         else
-          due[i] = due[i] + vol;  // Maxwell: du += ... (3d_maxwell.jl:229)
+          due[i] = due[i] + vol;  // Maxwell: du += ... (3d_maxwell.jl:229); advection :38-40
       }
+      if constexpr (NF == 1)
+        for (int i = 0; i < Np; ++i) due[i] = V::zero() - due[i];  // du = -du / J (:41)
       // du ./= J[1,1]  (3d_wave.jl:83)
       for (int i = 0; i < Np; ++i) due[i] = due[i] / J;
     }
@@ -517,12 +531,16 @@ void oracle_lift_f32(int N, int K, const float* x, float* out, int nthreads) {
   lift_matrix<float>(N, K, x, out, nthreads);
 }
 
-// phys: 0 = wave (4 fields), 1 = Maxwell (6 fields). q/du are AoS Np x K of SVector{nf}.
+// phys: 0 = wave (4 fields), 1 = Maxwell (6 fields), 2 = scalar advection (1 field,
+// examples/3d_advec_scalar.jl). q/du are AoS Np x K of SVector{nf}.
 int oracle_rhs_f64(int phys, int N, int K, const double* q, double* du, const int* Fmask,
                    const int64_t* mapP, const double* geo9, const double* nJ, double J,
                    double tau, int nthreads) {
   if (phys == 0)
     rhs_example<double, 4>(N, K, (const SV<double, 4>*)q, (SV<double, 4>*)du, Fmask, mapP,
+                           geo9, nJ, J, tau, nthreads);
+  else if (phys == 2)
+    rhs_example<double, 1>(N, K, (const SV<double, 1>*)q, (SV<double, 1>*)du, Fmask, mapP,
                            geo9, nJ, J, tau, nthreads);
   else if (phys == 1)
     rhs_example<double, 6>(N, K, (const SV<double, 6>*)q, (SV<double, 6>*)du, Fmask, mapP,
@@ -536,6 +554,8 @@ int oracle_rhs_f32(int phys, int N, int K, const float* q, float* du, const int*
                    float tau, int nthreads) {
   if (phys == 0)
     rhs_example<float, 4>(N, K, (const SV<float, 4>*)q, (SV<float, 4>*)du, Fmask, mapP, geo9, nJ, J, tau, nthreads);
+  else if (phys == 2)
+    rhs_example<float, 1>(N, K, (const SV<float, 1>*)q, (SV<float, 1>*)du, Fmask, mapP, geo9, nJ, J, tau, nthreads);
   else if (phys == 1)
     rhs_example<float, 6>(N, K, (const SV<float, 6>*)q, (SV<float, 6>*)du, Fmask, mapP, geo9, nJ, J, tau, nthreads);
   else
@@ -548,6 +568,8 @@ int oracle_lsrk_f64(int phys, int N, int K, double* q, double* res, const int* F
                     double tau, double dt, int nsteps, int nthreads) {
   if (phys == 0)
     lsrk_run<double, 4>(N, K, (SV<double, 4>*)q, (SV<double, 4>*)res, Fmask, mapP, geo9, nJ, J, tau, dt, nsteps, nthreads);
+  else if (phys == 2)
+    lsrk_run<double, 1>(N, K, (SV<double, 1>*)q, (SV<double, 1>*)res, Fmask, mapP, geo9, nJ, J, tau, dt, nsteps, nthreads);
   else if (phys == 1)
     lsrk_run<double, 6>(N, K, (SV<double, 6>*)q, (SV<double, 6>*)res, Fmask, mapP, geo9, nJ, J, tau, dt, nsteps, nthreads);
   else
@@ -559,6 +581,9 @@ int oracle_lsrk_f32(int phys, int N, int K, float* q, float* res, const int* Fma
                     float tau, float dt, int nsteps, int nthreads) {
   if (phys == 0)
     lsrk_run<float, 4>(N, K, (SV<float, 4>*)q, (SV<float, 4>*)res, Fmask, mapP, geo9, nJ, J,
+                       tau, dt, nsteps, nthreads);
+  else if (phys == 2)
+    lsrk_run<float, 1>(N, K, (SV<float, 1>*)q, (SV<float, 1>*)res, Fmask, mapP, geo9, nJ, J,
                        tau, dt, nsteps, nthreads);
   else if (phys == 1)
     lsrk_run<float, 6>(N, K, (SV<float, 6>*)q, (SV<float, 6>*)res, Fmask, mapP, geo9, nJ, J,

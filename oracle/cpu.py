@@ -114,7 +114,8 @@ def aos_to_soa(q: np.ndarray) -> np.ndarray:
 
 def rhs(phys: int, N: int, q_soa: np.ndarray, md, tau: float = 0.0,
         nthreads: int = 0) -> np.ndarray:
-    """Example right-hand side (wave phys=0, Maxwell phys=1) on SoA state (nf, K, Np).
+    """Example right-hand side (wave phys=0, Maxwell phys=1, scalar advection phys=2,
+    examples/3d_advec_scalar.jl) on SoA state (nf, K, Np).
 
     tau <= 0 evaluates the examples' flux as written; tau > 0 scales the penalty by the
     face Jacobian (upwind penalty tau).

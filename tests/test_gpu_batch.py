@@ -11,7 +11,7 @@ def specs():
     from bbdg.batch import ProblemSpec
     return [ProblemSpec("wave", 2, 2, seed=1), ProblemSpec("maxwell", 3, 2, seed=2),
             ProblemSpec("wave", 5, 3, seed=3), ProblemSpec("maxwell", 4, 2, seed=4),
-            ProblemSpec("wave", 9, 2, seed=5)]
+            ProblemSpec("advection", 6, 2, seed=6), ProblemSpec("wave", 9, 2, seed=5)]
 
 
 def test_batch_matches_single_solves_and_oracle(cuda, bb):
@@ -32,7 +32,8 @@ def test_batch_matches_single_solves_and_oracle(cuda, bb):
         s.run(q, r, B.dt(p), 3, graph=False)
         torch.cuda.synchronize()
         assert torch.equal(q, B.q[p]), p          # same tile code -> bitwise equal
-        want, _ = cpu.lsrk(0 if spec.physics == "wave" else 1, spec.N, q0[p].cpu().numpy(),
+        code = {"wave": 0, "maxwell": 1, "advection": 2}[spec.physics]
+        want, _ = cpu.lsrk(code, spec.N, q0[p].cpu().numpy(),
                            meshdata.build(mesh, spec.N), B.dt(p), 3, tau=spec.tau)
         got = B.q[p].cpu().numpy()
         for f in range(got.shape[0]):

@@ -189,3 +189,21 @@ def test_projection_operator_definition():
         c = rng.standard_normal(MN.shape[0])
         r = c - E @ (P @ c)                                           # residual is orthogonal
         assert np.abs(E.T @ MN @ r).max() < 1e-10 * np.abs(c).max()
+
+
+def test_advection_example_analytic_solution(oracle_cpu, bb):
+    """examples/3d_advec_scalar.jl end check: u0 = sin(pi x) sin(pi y) sin(pi z) advected in x
+    with unit speed on the periodic 4^3 hex mesh, N = 7, T = 0.1; L-inf error vs u0(x - T)."""
+    m = bb.uniform_tet_mesh(4)
+    N = 7
+    md = meshdata.build(m, N)
+    f0 = lambda x, y, z: np.sin(np.pi * x) * np.sin(np.pi * y) * np.sin(np.pi * z)
+    q = bb.project_fields(m, N, [f0])
+    T, nsteps = 0.1, 100
+    qT, _ = oracle_cpu.lsrk(2, N, q, md, T / nsteps, nsteps)
+    X = bb.element_domain_points(m, N)
+    x, y, z = X[..., 0], X[..., 1], X[..., 2]
+    V = bb.bernstein_basis_tet(N, *(2 * bb.mesh.reference_domain_points(N)[:, [1, 2, 3]].T - 1))
+    u = np.einsum("pn,kn->kp", V, qT[0])
+    ex = np.sin(np.pi * (x - T)) * np.sin(np.pi * y) * np.sin(np.pi * z)
+    assert np.abs(u - ex).max() < 1e-3
