@@ -22,6 +22,13 @@ CANDIDATES = {
                                  ("specialised", 2, 160), ("generic", 4, 256)],
     ("maxwell", 9, torch.float32): [("specialised", 2, 192), ("specialised", 2, 256),
                                     ("generic", 2, 256)],
+    ("wave", 5, torch.float32): [("specialised", 4, 160), ("specialised", 8, 320),
+                                 ("generic", 8, 256)],
+    ("maxwell", 5, torch.float32): [("specialised", 4, 224), ("specialised", 8, 448),
+                                    ("generic", 8, 256)],
+    ("wave", 10, torch.float32): [("specialised", 2, 160), ("generic", 4, 256)],
+    ("maxwell", 10, torch.float32): [("specialised", 2, 192), ("specialised", 2, 256),
+                                     ("generic", 2, 256)],
 }
 GENERIC = [("generic", e, 256) for e in (1, 2, 4, 6, 12)]
 
@@ -95,6 +102,23 @@ def tune(solver, steps: int = 3, use_cache: bool = True, verbose: bool = False):
 
 
 BATCH_TILES = (1, 2, 4, 6, 8)
+# The batched kernel runs every tile with the largest tile's shared memory; keeping tiles at
+# or below this leaves three resident blocks per SM for all problems.
+BATCH_TILE_BYTES = 72 * 1024
+
+
+def tile_bytes(physics: str, N: int, dtype, epb: int) -> int:
+    """Shared memory of one generic-kernel tile (bb_stage_tile_bytes)."""
+    import ctypes
+    from . import _lib
+    from .solver import PHYSICS
+    from .context import dtype_code
+    b, c = ctypes.c_int64(), ctypes.c_int()
+    rc = _lib.load().bb_stage_tile_bytes(PHYSICS[physics][0], int(N), dtype_code(dtype),
+                                         int(epb), ctypes.byref(b), ctypes.byref(c))
+    if rc != 0:
+        raise ValueError("bad tile description")
+    return int(b.value)
 
 
 def tune_batch(batch, steps: int = 2, verbose: bool = False):
@@ -116,7 +140,9 @@ def tune_batch(batch, steps: int = 2, verbose: bool = False):
                        device=batch.device) * 1e-3
         r = torch.zeros_like(q)
         times = {}
-        for epb in BATCH_TILES:
+        fits = [e for e in BATCH_TILES
+                if tile_bytes(physics, N, batch.dtype, e) <= BATCH_TILE_BYTES] or [1]
+        for epb in fits:
             try:
                 solver.set_tile(epb, 256)
             except Exception:

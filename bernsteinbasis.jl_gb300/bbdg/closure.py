@@ -31,7 +31,7 @@ from .mesh import TetMesh
 from .mlp import MLP, closure_apply, closure_features, transpose_bf16
 from .ordering import np2, np3
 from .solver import DGSolver
-from . import _lib
+from . import _lib, autotune
 from .context import get_context, ptr, stream_handle
 
 NF = 6  # Maxwell fields
@@ -77,6 +77,7 @@ class Closure:
             raise ValueError("the closure trains on whole snapshots: K must be a multiple of 8 "
                              "(an even number of hexahedra per side)")
         self.lo = DGSolver(mesh, cfg.N_lo, "maxwell", torch.float32, cfg.tau, device)
+        autotune.tune(self.lo)
         self.hi = None
         self.device = self.lo.device
         self.dt_hi = 0.25 * mesh.h / (cfg.N_hi + 1) ** 2
@@ -111,6 +112,7 @@ class Closure:
         if self.hi is None:
             self.hi = DGSolver(self.mesh, self.cfg.N_hi, "maxwell", torch.float32, self.cfg.tau,
                                self.device)
+            autotune.tune(self.hi)
         return self.hi
 
     def initial_state(self, seed: int, solver: DGSolver | None = None) -> torch.Tensor:

@@ -62,7 +62,8 @@ __global__ void __launch_bounds__(kBatchThreads, 3)
           s_phys = d.physics;
           s_begin = d.tile_begin;
           const int NF = physics_nf(d.physics);
-          sL = tile_layout_for(d.P.tab.N, NF, NF, sizeof(T), d.P.tab.nwords, d.P.epb);
+          sL = tile_layout_for(d.P.tab.N, NF, NF, sizeof(T), d.P.tab.nwords, d.P.epb,
+                               kBatchChainLiftBytes);
           s_prob = p;
           s_reload = 1;
         }
@@ -130,7 +131,7 @@ int batch_tile_default(int N, int nf, int dtype) {
   // largest of 6, 4, 2, 1 elements whose generic tile fits in 100 KB of shared memory
   const int cands[4] = {6, 4, 2, 1};
   for (int e : cands) {
-    const TileLayout L = tile_layout_for(N, nf, nf, dtype_size(dtype), 1 << 12, e);
+    const TileLayout L = tile_layout_for(N, nf, nf, dtype_size(dtype), 1 << 12, e, kBatchChainLiftBytes);
     if (L.total <= 100 * 1024) return e;
   }
   return 1;
@@ -175,7 +176,8 @@ int build_desc(bb_batch* b) {
     d.physics = pr.physics;
     begin += (pr.K + b->epb[p] - 1) / b->epb[p];
     const int nf = physics_nf(pr.physics);
-    const TileLayout L = tile_layout_for(pr.N, nf, nf, sizeof(T), t->nwords, b->epb[p]);
+    const TileLayout L = tile_layout_for(pr.N, nf, nf, sizeof(T), t->nwords, b->epb[p],
+                                         kBatchChainLiftBytes);
     smem = std::max(smem, L.total);
   }
   if (smem > ctx->smem_optin) return bb_fail(ctx, BB_ERR_ARG, "batch tiles exceed shared memory");
@@ -345,7 +347,8 @@ extern "C" int bb_batch_set_tile(bb_batch* b, int physics, int N, int elems_per_
   if (elems_per_block < 1 || elems_per_block > 64)
     return bb_fail(b->ctx, BB_ERR_ARG, "elements per block must be 1..64");
   const int nf = physics_nf(physics);
-  const TileLayout L = tile_layout_for(N, nf, nf, dtype_size(b->dtype), 1 << 12, elems_per_block);
+  const TileLayout L = tile_layout_for(N, nf, nf, dtype_size(b->dtype), 1 << 12, elems_per_block,
+                                         kBatchChainLiftBytes);
   if (L.total > b->ctx->smem_optin)
     return bb_fail(b->ctx, BB_ERR_ARG, "tile of %d elements exceeds shared memory", elems_per_block);
   int hits = 0;

@@ -57,6 +57,7 @@ struct DegTables {
                      // starts at np3(n-1)
   int o_fvol = 0;    // 4*Nfp uint16: face node -> volume index
   int o_fperm = 0;   // 6*Nfp uint16: face node -> neighbour face node, per orientation
+  int o_fstack = 0;  // 4*Np uint16: face f's lift stack entry (layer, node) -> volume index
   int nwords = 0;
   uint32_t* d_words = nullptr;
   double* d_lj = nullptr;  // N+1 entries, d_lj[j] = l_j(N) (constants.jl:10-12), [0] = 0
@@ -125,6 +126,7 @@ struct SmemTables {
   const uint16_t* node2;
   const uint16_t* fvol;
   const uint16_t* fperm;
+  const uint16_t* fstack;
 };
 
 // Shared-memory view of tables already copied to `s`.
@@ -135,6 +137,7 @@ __device__ __forceinline__ SmemTables tables_view(const DegTables& t, const uint
   r.node2 = reinterpret_cast<const uint16_t*>(s + t.o_node2);
   r.fvol = reinterpret_cast<const uint16_t*>(s + t.o_fvol);
   r.fperm = reinterpret_cast<const uint16_t*>(s + t.o_fperm);
+  r.fstack = reinterpret_cast<const uint16_t*>(s + t.o_fstack);
   return r;
 }
 
@@ -148,6 +151,7 @@ __device__ __forceinline__ SmemTables load_tables(const DegTables& t, const uint
   r.node2 = reinterpret_cast<const uint16_t*>(s + t.o_node2);
   r.fvol = reinterpret_cast<const uint16_t*>(s + t.o_fvol);
   r.fperm = reinterpret_cast<const uint16_t*>(s + t.o_fperm);
+  r.fstack = reinterpret_cast<const uint16_t*>(s + t.o_fstack);
   return r;
 }
 
@@ -199,64 +203,85 @@ __device__ __forceinline__ void copy_s2g(T* __restrict__ g, const T* __restrict_
 // Rounds a shared-memory byte offset up to 16 bytes.
 __host__ __device__ __forceinline__ size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
+// Rounded product (never fused into a following add), so that "out += w * v" gives the same
+// bits whether the product is stored first or added at once.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
+// L0 x at face node (i, j) of degree N, k = N - i - j: the 7-point stencil of
+// (N+1)^2/2 R_{N+1} E_{N->N+1} (src/BernsteinLift.jl:100-125 then :66-90 with the L0
+// scaling), x in the 2D layout of degree N with row offsets rb (row j), rbn (row j+1) and
+// rbp (row j-1). Shared by the level-parallel and the chain-per-thread lifts so that both
+// give the same bits.
+template <class T>
+__device__ __forceinline__ T l0_point(int i, int j, int k, const T* x, int rb, int rbn, int rbp) {
+  T v = T((i + 1) * (i + 1) + (j + 1) * (j + 1) + (k + 1) * (k + 1)) * x[rb + i];
+  if (j > 0) v = fma(T((i + 1) * j), x[rbp + i + 1], v);  // x(i+1, j-1)
+  if (k > 0) v = fma(T((i + 1) * k), x[rb + i + 1], v);   // x(i+1, j)
+  if (i > 0) v = fma(T((j + 1) * i), x[rbn + i - 1], v);  // x(i-1, j+1)
+  if (k > 0) v = fma(T((j + 1) * k), x[rbn + i], v);      // x(i, j+1)
+  if (i > 0) v = fma(T((k + 1) * i), x[rb + i - 1], v);   // x(i-1, j)
+  if (j > 0) v = fma(T((k + 1) * j), x[rbp + i], v);      // x(i, j-1)
+  return mul_rn(T(0.5), v);
+}
+
+// reduction_multiply! (src/BernsteinLift.jl:81-85) at output (i, j) from degree n:
+// ((i+1) x(i+1,j) + (j+1) x(i,j+1) + (n-i-j) x(i,j)) / n.
+template <class T>
+__device__ __forceinline__ T reduce_point(int i, int j, int n, T x_ip, T x_jp, T x_0, T inv) {
+  return fma(T(i + 1), x_ip, fma(T(j + 1), x_jp, T(n - i - j) * x_0)) * inv;
+}
+
 // One face's recursive lift, accumulated into a shared-memory volume block, for `ne`
 // elements and `nfld` fields at once (src/BernsteinLift.jl:139-164 applied per face and
 // summed through the permutations of :207-218):
-//   F = E_{N->N+1} x;  E0 = (N+1)^2/2 * R_{N+1} F;  layer 0 += E0;
-//   E_d = R_{N-d+1} E_{d-1};  layer d += l_d E_d   (d = 1..N)
+//   layer 0 += E_0 = L0 x (7-point stencil);  E_d = R_{N-d+1} E_{d-1};  layer d += l_d E_d
 // Level-parallel: one thread per output coefficient, a block barrier between levels, and
 // two ping-pong buffers (the reference's in-place reduction is not parallel-safe).
 //   in(le, fld)  : Nfp face coefficients at in + (le*in_es + fld*in_fs)
 //   out(le, fld) : Np volume coefficients at out + (le*out_es + fld*out_fs)
-//   bufA/bufB    : ne*nfld*np2(N+1) scratch each
+//   bufA/bufB    : ne*nfld*np2(N) scratch each
 // All threads of the block must call it.
 template <class T>
 __device__ void lift_face_accumulate(int N, int f, int ne, int nfld, const uint16_t* node2,
                                      const T* in, int in_es, int in_fs, T* out, int out_es,
                                      int out_fs, T* bufA, T* bufB, const T* lj) {
-  const int S = np2(N + 1);
+  const int S = np2(N);
   const int nchain = ne * nfld;
-  // elevation, degree N -> N+1 (src/BernsteinLift.jl:100-125)
+  // level 0: the L0 stencil on the degree-N face values
   {
-    const int n = N + 1;
-    const int cnt = np2(n);
-    const uint16_t* dec = node2 + np3(n - 1);
-    const T inv = T(1) / T(n);
-    for (int it = threadIdx.x; it < nchain * cnt; it += blockDim.x) {
-      const int ch = it / cnt, m = it - ch * cnt;
+    const uint16_t* dec = node2 + np3(N - 1);
+    for (int it = threadIdx.x; it < nchain * S; it += blockDim.x) {
+      const int ch = it / S, m = it - ch * S;
       const int le = ch / nfld, fld = ch - le * nfld;
       const T* x = in + le * in_es + fld * in_fs;
-      const int a = dec[m] & 0xff, b = dec[m] >> 8, c = n - a - b;
-      T val = T(0);
-      if (a > 0) val = T(a) * x[ij2(N, a - 1, b)];
-      if (b > 0) val = fma(T(b), x[ij2(N, a, b - 1)], val);
-      if (c > 0) val = fma(T(c), x[ij2(N, a, b)], val);
-      bufA[ch * S + m] = val * inv;
+      const int a = dec[m] & 0xff, b = dec[m] >> 8, c = N - a - b;
+      const int rb = tri_off(N, b);
+      const T e = l0_point<T>(a, b, c, x, rb, rb + (N + 1 - b), rb - (N + 2 - b));
+      bufA[ch * S + m] = e;
+      T* o = out + le * out_es + fld * out_fs;
+      o[face_vol(N, f, a, b, 0)] += e;
     }
   }
   __syncthreads();
-  // reduction chain: level 0 is the L0 apply (degree N+1 -> N, scaled by (N+1)^2/2)
   T* src = bufA;
   T* dst = bufB;
-  for (int d = 0; d <= N; ++d) {
+  for (int d = 1; d <= N; ++d) {
     const int n = N + 1 - d;         // input degree
     const int cnt = np2(n - 1);      // outputs
     const uint16_t* dec = node2 + np3(n - 2);
     const T inv = T(1) / T(n);
-    const T scale = (d == 0) ? T((N + 1) * (N + 1)) / T(2) : T(1);
-    const T wl = (d == 0) ? T(1) : lj[d];
+    const T wl = lj[d];
     for (int it = threadIdx.x; it < nchain * cnt; it += blockDim.x) {
       const int ch = it / cnt, m = it - ch * cnt;
       const int le = ch / nfld, fld = ch - le * nfld;
       const int a = dec[m] & 0xff, b = dec[m] >> 8;
       const T* x = src + ch * S;
-      // reduction_multiply! (src/BernsteinLift.jl:81-85)
-      T val = fma(T(a + 1), x[ij2(n, a + 1, b)],
-                  fma(T(b + 1), x[ij2(n, a, b + 1)], T(n - a - b) * x[ij2(n, a, b)]));
-      val = (val * inv) * scale;
+      const T val = reduce_point<T>(a, b, n, x[ij2(n, a + 1, b)], x[ij2(n, a, b + 1)],
+                                    x[ij2(n, a, b)], inv);
       dst[ch * S + m] = val;
       T* o = out + le * out_es + fld * out_fs;
-      o[face_vol(N, f, a, b, d)] += wl * val;
+      o[face_vol(N, f, a, b, d)] += mul_rn(wl, val);
     }
     __syncthreads();
     T* tmp = src;

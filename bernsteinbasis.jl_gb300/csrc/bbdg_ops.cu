@@ -108,6 +108,7 @@ const DegTables* bb_tables(bb_ctx* ctx, int N) {
   t->o_node2 = off; off += (n2 + 1) / 2;
   t->o_fvol = off; off += (4 * t->Nfp + 1) / 2;
   t->o_fperm = off; off += (6 * t->Nfp + 1) / 2;
+  t->o_fstack = off; off += (4 * t->Np + 1) / 2;
   t->nwords = off;
   std::vector<uint32_t> w(off, 0u);
   auto put16 = [&](int word_off, int idx, int v) {
@@ -141,6 +142,14 @@ const DegTables* bb_tables(bb_ctx* ctx, int N) {
         for (int v = 0; v < 3; ++v) wn[perm_of(o, v)] = wgt[v];
         put16(t->o_fperm, o * t->Nfp + q++, ij2(N, wn[0], wn[1]));
       }
+  }
+  // face f's lift stack in stack order (layer d outer, then j, then i, i + j <= N - d) ->
+  // volume index of the coefficient it lands on
+  for (int f = 0; f < 4; ++f) {
+    int q = 0;
+    for (int d = 0; d <= N; ++d)
+      for (int b = 0; b <= N - d; ++b)
+        for (int a = 0; a <= N - d - b; ++a) put16(t->o_fstack, f * t->Np + q++, face_vol(N, f, a, b, d));
   }
   std::vector<double> lj(N + 1, 0.0);
   std::vector<float> ljf(N + 1, 0.f);

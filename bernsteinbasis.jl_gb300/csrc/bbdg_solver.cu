@@ -84,7 +84,7 @@ struct bb_solver {
 
 namespace {
 
-int solver_layout(bb_solver* s, int epb, size_t* smem_out) {
+int solver_layout(bb_solver* s, int epb, size_t* smem_out, int* chain_out = nullptr) {
   TileLayout L;
   if (s->physics == BB_WAVE)
     L = s->dtype == BB_F64 ? tile_layout<double, BB_WAVE>(*s->tab, epb)
@@ -96,6 +96,7 @@ int solver_layout(bb_solver* s, int epb, size_t* smem_out) {
     L = s->dtype == BB_F64 ? tile_layout<double, BB_MAXWELL>(*s->tab, epb)
                            : tile_layout<float, BB_MAXWELL>(*s->tab, epb);
   *smem_out = L.total;
+  if (chain_out) *chain_out = L.chain;
   return L.total <= s->ctx->smem_optin ? BB_OK : BB_ERR_ARG;
 }
 
@@ -289,16 +290,20 @@ extern "C" int bb_solver_create(bb_ctx* ctx, int physics, int N, int64_t K, int 
   s->geo = geo;
   s->tau = tau;
   s->tab = t;
-  // default tile: the largest of 12, 6, 4, 2, 1 elements that fits in 100 KB of smem
+  // default tile: the largest of 12, 6, 4, 2, 1 elements whose tile runs the chain lift
+  // (fits in its shared-memory budget), else the largest that fits in 100 KB
   const int cands[5] = {12, 6, 4, 2, 1};
-  for (int c : cands) {
-    size_t sm = 0;
-    if (solver_layout(s, c, &sm) == BB_OK && sm <= 100 * 1024) {
-      s->epb = c;
-      s->smem = sm;
-      break;
+  for (int pass = 0; pass < 2 && !s->epb; ++pass)
+    for (int c : cands) {
+      size_t sm = 0;
+      int chain = 0;
+      if (solver_layout(s, c, &sm, &chain) == BB_OK && sm <= 100 * 1024 &&
+          (pass == 1 || chain)) {
+        s->epb = c;
+        s->smem = sm;
+        break;
+      }
     }
-  }
   if (!s->epb) {
     size_t sm = 0;
     if (solver_layout(s, 1, &sm) != BB_OK) {
@@ -390,6 +395,21 @@ extern "C" int bb_solver_set_kernel(bb_solver* s, int kind) {
 
 extern "C" int bb_solver_get_kernel(const bb_solver* s) {
   return s ? (s->fast >= 0 ? 0 : 1) : -1;
+}
+
+extern "C" int bb_stage_tile_bytes(int physics, int N, int dtype, int epb, int64_t* bytes,
+                                   int* chain) {
+  if (physics_nf(physics) == 0 || !valid_degree(N) || !valid_dtype(dtype) || epb < 1 ||
+      epb > 64 || !bytes)
+    return BB_ERR_ARG;
+  // table words of degree N: node3, node3m1, node2 (u16), fvol, fperm, fstack (u16)
+  const int nwords = np3(N) + np3(N - 1) + (np3(N + 1) + 1) / 2 + (4 * np2(N) + 1) / 2 +
+                     (6 * np2(N) + 1) / 2 + (4 * np3(N) + 1) / 2;
+  const int nf = physics_nf(physics);
+  const TileLayout L = tile_layout_for(N, nf, nf, dtype_size(dtype), nwords, epb);
+  *bytes = (int64_t)L.total;
+  if (chain) *chain = L.chain;
+  return BB_OK;
 }
 
 extern "C" int bb_solver_get_tile(const bb_solver* s, int* epb, int* threads) {

@@ -92,6 +92,9 @@ struct FastLayout {
   static constexpr int TF_B = (FNB_B + 24 * NFP * 2 + 15) / 16 * 16;   // [NP] u32 face nodes
   static constexpr int BAR_B = (TF_B + NP * 4 + 15) / 16 * 16;         // 3 mbarriers
   static constexpr int BYTES = BAR_B + 32;
+  // resident blocks per SM the register budget is sized for (2 when two tiles fit in the
+  // shared memory of an SM, else 1)
+  static constexpr int MINB = 2 * BYTES <= 227 * 1024 ? 2 : 1;
   static_assert((EPB * NP * 4) % 16 == 0, "tile segments must be multiples of 16 bytes");
   static_assert(NFP < 255, "face node indices are packed in bytes");
   static_assert(TPE % 32 == 0 && TPE >= 32, "element threads come in whole warps");
@@ -205,7 +208,8 @@ __device__ __forceinline__ void lift_chain(const float* x, float* g) {
 }
 
 template <int N, int PHYS, int EPB, int TPE>
-__global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT, 2)
+__global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
+                                  FastLayout<N, PHYS, EPB, TPE>::MINB)
     stage_fast_kernel(FastStageParams P) {
   using L = FastLayout<N, PHYS, EPB, TPE>;
   constexpr int NP = L::NP, NFP = L::NFP, NPM1 = L::NPM1, NF = L::NF, NCH = L::NCH;
@@ -489,8 +493,16 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT, 2)
       if (pre) {
         const int64_t nb = (int64_t)((uint32_t)cpre >> 5);
         const int nfc = (cpre >> 3) & 3;
-        if (nb < K && (nb < tpre * EPB || nb >= (tpre + 1) * EPB))
-          l2_prefetch(P.trace_in + ((size_t)nb * 4 + nfc) * NF * NFP, NF * NFP * 4);
+        if (nb < K && (nb < tpre * EPB || nb >= (tpre + 1) * EPB)) {
+          // the bulk prefetch wants a 16-byte aligned start and size; a face block
+          // (NF * NFP floats) need not be, so widen it to 16-byte boundaries. The trace
+          // buffer starts on such a boundary and its length (16 K NF NFP bytes) is a
+          // multiple of 16, so the widened range stays inside it.
+          const uintptr_t a0 = (uintptr_t)(P.trace_in + ((size_t)nb * 4 + nfc) * NF * NFP);
+          const uintptr_t lo = a0 & ~(uintptr_t)15;
+          const uintptr_t hi = (a0 + (uintptr_t)(NF * NFP * 4) + 15) & ~(uintptr_t)15;
+          l2_prefetch(reinterpret_cast<const void*>(lo), (uint32_t)(hi - lo));
+        }
       }
       if (tnext < ntiles) {
         if (!mbar_wait(&bar[s ^ 1], (ph >> (s ^ 1)) & 1u)) s_fail = 1;
@@ -656,7 +668,14 @@ int launch_fast_t(const FastLaunch& fl, const FastStageParams& P, cudaStream_t s
   X(9, BB_WAVE, 4, 32)      \
   X(9, BB_WAVE, 2, 64)      \
   X(9, BB_MAXWELL, 2, 64)   \
-  X(9, BB_MAXWELL, 2, 96)
+  X(9, BB_MAXWELL, 2, 96)   \
+  X(5, BB_WAVE, 4, 32)      \
+  X(5, BB_WAVE, 8, 32)      \
+  X(5, BB_MAXWELL, 4, 32)   \
+  X(5, BB_MAXWELL, 8, 32)   \
+  X(10, BB_WAVE, 2, 64)     \
+  X(10, BB_MAXWELL, 2, 64)  \
+  X(10, BB_MAXWELL, 2, 96)
 
 // The public tile description is (elements per block, threads per block).
 int bb_fast_find(int N, int physics, int epb, int threads, int64_t K) {

@@ -60,16 +60,23 @@ struct StageParams {
   int* status;          // device error word
 };
 
-// Shared-memory layout of a tile (in units of T unless noted).
+// Shared-memory layout of a tile (in units of T unless noted). chain != 0: the lift runs one
+// thread per (element, face, field) chain with the face stacks in shared memory (used when
+// that fits in kChainLiftBytes); chain == 0: the level-parallel lift with two ping-pong rows.
 struct TileLayout {
   size_t q, out, flux, work, geo, lj, conn_bytes, tab_bytes, total;
   int work_elems;
+  int chain;
 };
+constexpr size_t kChainLiftBytes = 100 * 1024;
+// The batched kernel uses the same rule, so that a tile timed on a single problem (how its
+// size is chosen per physics and degree) runs the same code inside the batch.
+constexpr size_t kBatchChainLiftBytes = kChainLiftBytes;
 
 // Layout for degree N with Np/Nfp/NpM1 coefficients, NF fields, NW volume terms, scalars of
 // `tsize` bytes and `nwords` 32-bit table words.
-__host__ __device__ inline TileLayout tile_layout_for(int N, int NF, int NW, size_t tsize,
-                                                     int nwords, int epb) {
+__host__ __device__ inline TileLayout tile_layout_with(int N, int NF, int NW, size_t tsize,
+                                                      int nwords, int epb, int chain) {
   TileLayout L;
   const size_t Np = np3(N), Nfp = np2(N), NpM1 = np3(N - 1), S = np2(N + 1);
   size_t off = 0;
@@ -77,7 +84,9 @@ __host__ __device__ inline TileLayout tile_layout_for(int N, int NF, int NW, siz
   L.out = off; off += (size_t)NF * epb * Np;
   L.flux = off; off += (size_t)epb * 4 * NF * Nfp;
   L.work = off;
-  const size_t wvol = (size_t)NW * epb * NpM1, wlift = 2 * (size_t)epb * NF * S;
+  const size_t wvol = (size_t)NW * epb * NpM1;
+  const size_t wlift = chain ? (size_t)epb * 4 * NF * (Np + (Nfp | 1))  // stacks + rows
+                             : 2 * (size_t)epb * NF * S;
   L.work_elems = (int)(wvol > wlift ? wvol : wlift);
   off += L.work_elems;
   L.geo = off; off += (size_t)epb * BB_GEO_STRIDE;
@@ -86,7 +95,56 @@ __host__ __device__ inline TileLayout tile_layout_for(int N, int NF, int NW, siz
   L.conn_bytes = bytes; bytes += align16((size_t)epb * 4 * sizeof(int32_t));
   L.tab_bytes = bytes; bytes += (size_t)nwords * 4;
   L.total = align16(bytes);
+  L.chain = chain;
   return L;
+}
+
+// The chain lift when its tile fits in `budget` bytes, else the level-parallel one.
+__host__ __device__ inline TileLayout tile_layout_for(int N, int NF, int NW, size_t tsize,
+                                                     int nwords, int epb,
+                                                     size_t budget = kChainLiftBytes) {
+  const TileLayout c = tile_layout_with(N, NF, NW, tsize, nwords, epb, 1);
+  return c.total <= budget ? c : tile_layout_with(N, NF, NW, tsize, nwords, epb, 0);
+}
+
+// One face lift chain for run-time N, one thread (src/BernsteinLift.jl:139-164):
+//   E_0 = L0 x (the 7-point stencil of (N+1)^2/2 R_{N+1} E_{N->N+1}), E_d = R_{N-d+1} E_{d-1}
+// in place in ascending order on the thread's shared-memory row E (degree-N layout), and
+// l_d E_d written to the face's stack g in volume order through the stack table fst
+// (face f's entries: layer d, then j, then i, i + j <= N - d).
+template <class T>
+__device__ void chain_lift_runtime(int N, const T* __restrict__ x, T* __restrict__ E,
+                                   T* __restrict__ g, const uint16_t* __restrict__ fst,
+                                   const T* __restrict__ lj) {
+  int rb = 0;  // row offset of row j in the degree-N triangle
+  for (int j = 0; j <= N; ++j) {
+    const int rlen = N + 1 - j;
+    const int rbn = rb + rlen;          // row j + 1
+    const int rbp = rb - (rlen + 1);    // row j - 1 (used only when j > 0)
+    for (int i = 0; i < rlen; ++i) {
+      const T e = l0_point<T>(i, j, N - i - j, x, rb, rbn, rbp);
+      E[rb + i] = e;
+      g[fst[rb + i]] = e;  // layer 0: stack index = 2D index
+    }
+    rb = rbn;
+  }
+  int s = rb;  // == np2(N): first entry of layer 1
+  for (int d = 1; d <= N; ++d) {
+    const int n = N - d + 1;  // input degree of this reduction
+    const T inv = T(1) / T(n);
+    const T w = lj[d];
+    int r = 0;
+    for (int j = 0; j < n; ++j) {
+      const int rn = r + (N + 1 - j);  // next row in the degree-N layout
+      for (int i = 0; i + j < n; ++i) {
+        // in place, ascending: (i+1, j) and (i, j+1) are still degree-n values
+        const T v = reduce_point<T>(i, j, n, E[r + i + 1], E[rn + i], E[r + i], inv);
+        E[r + i] = v;
+        g[fst[s++]] = mul_rn(w, v);
+      }
+      r = rn;
+    }
+  }
 }
 
 template <class T, int PHYS>
@@ -96,7 +154,7 @@ TileLayout tile_layout(const DegTables& t, int epb) {
 
 // One tile of the generic stage (all threads of the block call it). The degree tables are in
 // shared memory (st), sLj holds l_j(N); the layout L matches P's degree, physics and tile.
-template <class T, int PHYS>
+template <class T, int PHYS, bool CHAIN_LIFT = true>
 __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
                                    const SmemTables& st, int64_t tile) {
   constexpr int NF = Phys<PHYS>::NF, NW = Phys<PHYS>::NW;
@@ -288,7 +346,32 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
     __syncthreads();
 
     // ---- 4. lift of the face fluxes, face t=-1 first as src/BernsteinLift.jl:202-205 ----
-    {
+    if (CHAIN_LIFT && L.chain) {
+      // one thread per (element, face, field) chain; stacks land in volume order
+      const int nchain = ne * 4 * NF;
+      const int rs = Nfp | 1;
+      T* sStack = sWork;                                // [epb*4*NF][Np]
+      T* sRow = sWork + (size_t)epb * 4 * NF * Np;      // [epb*4*NF][rs]
+      for (int c = threadIdx.x; c < nchain; c += blockDim.x) {
+        const int f = (c / NF) & 3;                     // c = (le*4 + f)*NF + fld
+        chain_lift_runtime<T>(N, sFlux + (size_t)c * Nfp, sRow + (size_t)c * rs,
+                              sStack + (size_t)c * Np, st.fstack + (size_t)f * Np, sLj);
+      }
+      __syncthreads();
+      for (int it = threadIdx.x; it < ne * NF * Np; it += blockDim.x) {
+        const int le = it / (NF * Np), rem = it - le * NF * Np;
+        const int fld = rem / Np, n = rem - fld * Np;
+        const T* g = sStack + ((size_t)le * 4 * NF + fld) * Np + n;  // face f at + f*NF*Np
+        T* o = sOut + ((size_t)fld * epb + le) * Np + n;
+        T acc = *o;
+        acc += g[(size_t)3 * NF * Np];
+        acc += g[0];
+        acc += g[(size_t)1 * NF * Np];
+        acc += g[(size_t)2 * NF * Np];
+        *o = acc;
+      }
+      __syncthreads();
+    } else {
       const int order[4] = {3, 0, 1, 2};
       const int S = np2(N + 1);
       T* bufA = sWork;

@@ -113,6 +113,9 @@ int bb_solver_destroy(bb_solver* s);
  * registers, bulk-copy pipelined tiles); those need K to be a multiple of the tile. */
 int bb_solver_set_tile(bb_solver* s, int elems_per_block, int threads);
 int bb_solver_get_tile(const bb_solver* s, int* elems_per_block, int* threads);
+/* Shared memory of one generic-kernel tile of epb elements (and whether it runs the
+ * chain-per-thread lift), for tile choosers. */
+int bb_stage_tile_bytes(int physics, int N, int dtype, int epb, int64_t* bytes, int* chain);
 /* kind 0: use a degree-specialised kernel when one exists (default); 1: generic kernel. */
 int bb_solver_set_kernel(bb_solver* s, int kind);
 /* 0 if a degree-specialised kernel is in use, 1 for the generic kernel. */

@@ -162,7 +162,11 @@ def test_corrupt_connectivity_is_reported(cuda, bb):
 
 
 FAST_TILES = {("wave", 9): [(4, 288), (4, 160), (2, 160)],
-              ("maxwell", 9): [(2, 192), (2, 256)]}
+              ("maxwell", 9): [(2, 192), (2, 256)],
+              ("wave", 5): [(4, 160), (8, 320)],
+              ("maxwell", 5): [(4, 224), (8, 448)],
+              ("wave", 10): [(2, 160)],
+              ("maxwell", 10): [(2, 192), (2, 256)]}
 
 
 def pulse_fields(nf):
@@ -208,6 +212,31 @@ def test_degree_specialised_kernels_match_oracle_and_generic(cuda, bb, oracle_cp
         e1 = per_field_rel(qf.cpu().numpy(), q_or)
         e2 = per_field_rel(qf.cpu().numpy(), qg.cpu().numpy())
         assert np.all(e1 < 1e-5) and np.all(e2 < 1e-5), (epb, nt, e1, e2)
+
+
+@pytest.mark.parametrize("key", sorted(FAST_TILES))
+def test_degree_specialised_kernels_on_many_tiles(cuda, bb, key):
+    """Every variant on a mesh with many more tiles than blocks (K = 3,072), where each block
+    prefetches the neighbour traces of tiles ahead: equal to the generic kernel (1e-5)."""
+    import torch
+    physics, N = key
+    m = bb.uniform_tet_mesh(8)
+    s = bb.DGSolver(m, N, physics, dtype=torch.float32, tau=1.0)
+    q0 = bb.project_fields(m, N, pulse_fields(s.nf))
+    dt = s.dt_cfl()
+    s.set_kernel("generic")
+    s.set_tile(4, 256)
+    qg = torch.tensor(q0, dtype=torch.float32, device=cuda)
+    rg = torch.zeros_like(qg)
+    s.run(qg, rg, dt, 2)
+    s.set_kernel("specialised")
+    for epb, nt in FAST_TILES[key]:
+        s.set_tile(epb, nt)
+        qf = torch.tensor(q0, dtype=torch.float32, device=cuda)
+        rf = torch.zeros_like(qf)
+        s.run(qf, rf, dt, 2)
+        err = per_field_rel(qf.cpu().numpy(), qg.cpu().numpy())
+        assert np.all(err < 1e-5), (epb, nt, err)
 
 
 def test_specialised_kernel_falls_back_on_misaligned_state(cuda, bb, oracle_cpu):
