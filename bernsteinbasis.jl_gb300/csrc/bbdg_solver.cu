@@ -173,9 +173,10 @@ bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
 
 int launch_stage(bb_solver* s, int mode, int stage, double dt, void* q, void* res, void* rhs,
                  const void* tin, void* tout, cudaStream_t st) {
-  // the specialised kernels move tiles with 16-byte-aligned bulk copies
-  if (s->fast >= 0 && aligned16(q) && (!res || aligned16(res)) && aligned16(s->geo) &&
-      aligned16(s->conn))
+  // the specialised kernels move tiles with 16-byte-aligned bulk copies and store q, res
+  // and rhs with 16-byte vector stores
+  if (s->fast >= 0 && aligned16(q) && (!res || aligned16(res)) && (!rhs || aligned16(rhs)) &&
+      aligned16(s->geo) && aligned16(s->conn))
     return launch_fast(s, mode, stage, dt, q, res, rhs, tin, tout, st);
   if (s->physics == BB_WAVE)
     return s->dtype == BB_F64

@@ -254,6 +254,14 @@ def test_specialised_kernel_falls_back_on_misaligned_state(cuda, bb, oracle_cpu)
     assert qd.data_ptr() % 16 != 0
     err = per_field_rel(s.rhs(qd).cpu().numpy(), oracle_cpu.rhs(0, N, q, md, tau=1.0))
     assert np.all(err < 1e-5), err
+    # aligned state, output that does not start on a 16-byte boundary: also the generic path
+    qa = torch.tensor(q, dtype=torch.float32, device=cuda)
+    obuf = torch.empty(q.size + 1, dtype=torch.float32, device=cuda)
+    out = obuf[1:].view(q.shape)
+    assert out.data_ptr() % 16 != 0
+    s.rhs(qa, out=out)
+    err = per_field_rel(out.cpu().numpy(), oracle_cpu.rhs(0, N, q, md, tau=1.0))
+    assert np.all(err < 1e-5), err
 
 
 # ---- scalar advection (examples/3d_advec_scalar.jl) ----------------------------------------
