@@ -280,6 +280,9 @@ __global__ void __launch_bounds__(256) deriv_fact_kernel(DegTables tab,
   }
   for (int t = threadIdx.x; t < 3 * epb; t += blockDim.x) sW[(size_t)t * NW + NPM1] = T(0);
   T* outs[3] = {o0, o1, o2};
+  // it / d as (it * ceil(2^32 / d)) >> 32 (exact for it < 2^32 / d; d = 1 gives 2^32)
+  const uint64_t inv_m1 = 0xFFFFFFFFull / (uint64_t)NPM1 + 1ull;
+  const uint64_t inv_np = 0xFFFFFFFFull / (uint64_t)Np + 1ull;
   const int64_t nblk = (K + epb - 1) / epb;
   for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
     const int64_t e0 = blk * epb;
@@ -288,7 +291,7 @@ __global__ void __launch_bounds__(256) deriv_fact_kernel(DegTables tab,
     copy_g2s(sx, x + e0 * Np, ne * Np);
     __syncthreads();
     for (int it = threadIdx.x; it < ne * NPM1; it += blockDim.x) {
-      const int le = it / NPM1, b = it - le * NPM1;
+      const int le = (int)(((uint64_t)it * inv_m1) >> 32), b = it - le * NPM1;
       const uint2 vn = sVN[b];
       const T* xe = sx + (size_t)le * Np;
       const T x3 = xe[vn.y >> 16];
@@ -298,7 +301,7 @@ __global__ void __launch_bounds__(256) deriv_fact_kernel(DegTables tab,
     }
     __syncthreads();
     for (int it = threadIdx.x; it < ne * Np; it += blockDim.x) {
-      const int le = it / Np, n = it - le * Np;
+      const int le = (int)(((uint64_t)it * inv_np) >> 32), n = it - le * Np;
       const uint2 ga = sGA[n];
       const uint32_t gw = sGW[n];
       const int m0 = ga.x & 0xffff, m1 = ga.x >> 16, m2 = ga.y & 0xffff, m3 = ga.y >> 16;
