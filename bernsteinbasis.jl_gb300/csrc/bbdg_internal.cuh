@@ -13,6 +13,19 @@
 #include "../../include/bbdg.h"
 
 // ------------------------------------------------------------------------------------
+// Exact q = it / d for 0 <= it < 2^32 / d (d >= 1) by a multiply-high with ceil(2^32 / d):
+// the index loops divide a flat item number by runtime sizes on every iteration.
+struct FastDiv {
+  uint32_t m;
+  int d;
+  __host__ __device__ explicit FastDiv(int d_)
+      : m(d_ > 1 ? (uint32_t)(0xFFFFFFFFull / (uint64_t)d_ + 1ull) : 0u), d(d_) {}
+  __device__ __forceinline__ int div(int it) const {
+    return d > 1 ? (int)__umulhi((uint32_t)it, m) : it;
+  }
+};
+
+// ------------------------------------------------------------------------------------
 // Degree bookkeeping. Multi-indices follow src/ordering.jl: 3D coefficients are ordered
 // k (outer), j, i (inner); 2D coefficients j (outer), i (inner).
 // ------------------------------------------------------------------------------------
@@ -248,12 +261,14 @@ __device__ void lift_face_accumulate(int N, int f, int ne, int nfld, const uint1
                                      int out_fs, T* bufA, T* bufB, const T* lj) {
   const int S = np2(N);
   const int nchain = ne * nfld;
+  const FastDiv by_nfld(nfld);
   // level 0: the L0 stencil on the degree-N face values
   {
     const uint16_t* dec = node2 + np3(N - 1);
+    const FastDiv by_s(S);
     for (int it = threadIdx.x; it < nchain * S; it += blockDim.x) {
-      const int ch = it / S, m = it - ch * S;
-      const int le = ch / nfld, fld = ch - le * nfld;
+      const int ch = by_s.div(it), m = it - ch * S;
+      const int le = by_nfld.div(ch), fld = ch - le * nfld;
       const T* x = in + le * in_es + fld * in_fs;
       const int a = dec[m] & 0xff, b = dec[m] >> 8, c = N - a - b;
       const int rb = tri_off(N, b);
@@ -272,9 +287,10 @@ __device__ void lift_face_accumulate(int N, int f, int ne, int nfld, const uint1
     const uint16_t* dec = node2 + np3(n - 2);
     const T inv = T(1) / T(n);
     const T wl = lj[d];
+    const FastDiv by_cnt(cnt);
     for (int it = threadIdx.x; it < nchain * cnt; it += blockDim.x) {
-      const int ch = it / cnt, m = it - ch * cnt;
-      const int le = ch / nfld, fld = ch - le * nfld;
+      const int ch = by_cnt.div(it), m = it - ch * cnt;
+      const int le = by_nfld.div(ch), fld = ch - le * nfld;
       const int a = dec[m] & 0xff, b = dec[m] >> 8;
       const T* x = src + ch * S;
       const T val = reduce_point<T>(a, b, n, x[ij2(n, a + 1, b)], x[ij2(n, a, b + 1)],

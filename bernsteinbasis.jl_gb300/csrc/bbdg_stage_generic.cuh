@@ -170,6 +170,8 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
   const int N = P.tab.N, Np = P.tab.Np, NpM1 = P.tab.NpM1, Nfp = P.tab.Nfp;
   const int64_t K = P.K;
   const int epb = P.epb;
+  const FastDiv by_np(Np), by_npm1(NpM1), by_nfp(Nfp), by_4nfp(4 * Nfp), by_nfnp(NF * Np),
+      by_nfnfp(NF * Nfp), by_4nfnfp(4 * NF * Nfp);
     const int64_t e0 = tile * epb;
     const int ne = (int)min64(epb, K - e0);
     __syncthreads();
@@ -182,9 +184,9 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
 
     // ---- 2. interface flux -------------------------------------------------------------
     for (int it = threadIdx.x; it < ne * 4 * Nfp; it += blockDim.x) {
-      const int le = it / (4 * Nfp);
+      const int le = by_4nfp.div(it);
       const int rem = it - le * 4 * Nfp;
-      const int f = rem / Nfp, a = rem - f * Nfp;
+      const int f = by_nfp.div(rem), a = rem - f * Nfp;
       const int32_t c = sConn[le * 4 + f];
       const int64_t nbr = (int64_t)((uint32_t)c >> 5);
       const int nface = (c >> 3) & 3, o = c & 7;
@@ -257,7 +259,7 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
 
     // ---- 3a. volume term at degree N-1 -------------------------------------------------
     for (int it = threadIdx.x; it < ne * NpM1; it += blockDim.x) {
-      const int le = it / NpM1, b = it - le * NpM1;
+      const int le = by_npm1.div(it), b = it - le * NpM1;
       const uint32_t c = st.node3m1[b];
       const int i = c & 0xff, j = (c >> 8) & 0xff, k = c >> 16;
       const int idx[4] = {ijk3(N, i + 1, j, k), ijk3(N, i, j + 1, k), ijk3(N, i, j, k + 1),
@@ -311,7 +313,7 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
     __syncthreads();
     // ---- 3b. elevate back to degree N: out(alpha) = sign * sum_b alpha_b w(alpha - e_b) -
     for (int it = threadIdx.x; it < ne * Np; it += blockDim.x) {
-      const int le = it / Np, n = it - le * Np;
+      const int le = by_np.div(it), n = it - le * Np;
       const uint32_t c = st.node3[n];
       const int i = c & 0xff, j = (c >> 8) & 0xff, k = c >> 16, l = N - i - j - k;
       T acc[NW];
@@ -359,8 +361,8 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
       }
       __syncthreads();
       for (int it = threadIdx.x; it < ne * NF * Np; it += blockDim.x) {
-        const int le = it / (NF * Np), rem = it - le * NF * Np;
-        const int fld = rem / Np, n = rem - fld * Np;
+        const int le = by_nfnp.div(it), rem = it - le * NF * Np;
+        const int fld = by_np.div(rem), n = rem - fld * Np;
         const T* g = sStack + ((size_t)le * 4 * NF + fld) * Np + n;  // face f at + f*NF*Np
         T* o = sOut + ((size_t)fld * epb + le) * Np + n;
         T acc = *o;
@@ -389,7 +391,7 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
         T* dst = P.rhs + ((size_t)fld * K + e0) * Np;
         const T* src = sOut + (size_t)fld * epb * Np;
         for (int t = threadIdx.x; t < ne * Np; t += blockDim.x) {
-          const int le = t / Np;
+          const int le = by_np.div(t);
           dst[t] = src[t] * sGeo[le * BB_GEO_STRIDE + 9];
         }
       }
@@ -400,7 +402,7 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
         T* sq = sQ + (size_t)fld * epb * Np;
         const T* so = sOut + (size_t)fld * epb * Np;
         for (int t = threadIdx.x; t < ne * Np; t += blockDim.x) {
-          const int le = t / Np;
+          const int le = by_np.div(t);
           const T rhs = so[t] * sGeo[le * BB_GEO_STRIDE + 9];
           const T r = P.rkA * gr[t] + P.dt * rhs;
           const T qn = sq[t] + P.rkB * r;
@@ -412,11 +414,11 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
       if (P.trace_out) {
         __syncthreads();
         for (int it = threadIdx.x; it < ne * 4 * NF * Nfp; it += blockDim.x) {
-          const int le = it / (4 * NF * Nfp);
+          const int le = by_4nfnfp.div(it);
           int rem = it - le * 4 * NF * Nfp;
-          const int f = rem / (NF * Nfp);
+          const int f = by_nfnfp.div(rem);
           rem -= f * NF * Nfp;
-          const int fld = rem / Nfp, a = rem - fld * Nfp;
+          const int fld = by_nfp.div(rem), a = rem - fld * Nfp;
           const int64_t nbr = (int64_t)((uint32_t)sConn[le * 4 + f] >> 5);
           if (nbr >= e0 && nbr < e0 + ne) continue;  // neighbour inside the tile
           P.trace_out[((size_t)(e0 + le) * 4 + f) * NF * Nfp + (size_t)fld * Nfp + a] =
