@@ -185,7 +185,7 @@ def config4(steps: int = 100, dtype=torch.float32, compare_single: bool = True):
 def config5(n: int = 16, n_train: int = 16, nmacro_train: int = 40, epochs: int = 20,
             n_eval: int = 2, nmacro_eval: int = 40, seed: int = 3, lr: float = 1e-3,
             hidden=(512, 512), N_hi: int = 10, N_lo: int = 5, rollout_epochs: int = 0,
-            noise: float = 0.0):
+            noise: float = 0.0, store_gb: float = 40.0):
     """Closure training and held-out evaluation. Training initial conditions are drawn from
     `seed`, the held-out ones from seed + 1000; every number is measured on the GPU."""
     from .closure import Closure, ClosureConfig
@@ -205,6 +205,7 @@ def config5(n: int = 16, n_train: int = 16, nmacro_train: int = 40, epochs: int 
     cl.fit_scales(train_seeds[0], 3)
     info = cl.train(train_seeds, nmacro_train, epochs=epochs, lr=lr, lr_final=lr / 100,
                     rollout_epochs=rollout_epochs, noise=noise,
+                    store_limit_bytes=store_gb * 1e9,
                     log=lambda s: print(s, flush=True))
     info.update({"s_in": cl.s_in, "s_out": cl.s_out})
     print(json.dumps({"train": info}), flush=True)
@@ -244,6 +245,8 @@ def main():
     ap.add_argument("--N-lo", type=int, default=5)
     ap.add_argument("--rollout-epochs", type=int, default=0)
     ap.add_argument("--noise", type=float, default=0.0)
+    ap.add_argument("--store-gb", type=float, default=40.0,
+                    help="device memory for the training snapshot store (per phase)")
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--degrees", type=str, default="3-15")
     a = ap.parse_args()
@@ -258,7 +261,7 @@ def main():
         config5(n=a.n, n_train=a.n_train, nmacro_train=a.nmacro_train, epochs=a.epochs,
                 n_eval=a.n_eval, nmacro_eval=a.nmacro_eval, lr=a.lr,
                 hidden=tuple(int(v) for v in a.hidden.split(",")), N_hi=a.N_hi, N_lo=a.N_lo,
-                rollout_epochs=a.rollout_epochs, noise=a.noise)
+                rollout_epochs=a.rollout_epochs, noise=a.noise, store_gb=a.store_gb)
 
 
 if __name__ == "__main__":
