@@ -62,6 +62,8 @@ SIGNATURES = {
     "bb_mass_norms": (_I, [_P, _I, _I64, _I, _I, _P, _P, _P, ctypes.POINTER(_D), _P]),
     "bb_norms_noalloc": (_I, [_I, _I64, _I, _I, _P, _P, _P, _P]),
     "bb_project": (_I, [_P, _I, _I, _I64, _I, _I, _P, _I, _P, _P]),
+    "bb_conn_from_mapP": (_I, [_I, _I64, _P, _P, _P]),
+    "bb_geo_from_meshdata": (_I, [_I64, _I, _P, _P, _P, _P]),
 }
 
 class BatchProblem(ctypes.Structure):

@@ -173,3 +173,39 @@ def element_domain_points(mesh: TetMesh, N: int) -> np.ndarray:
     """Physical coordinates (K, Np, 3) of every element's degree-N domain points."""
     W = reference_domain_points(N)                     # (Np, 4) on X1..X4
     return np.einsum("pm,kmc->kpc", W, mesh.EVX)
+
+
+def from_meshdata(N: int, Fmask: np.ndarray, mapP: np.ndarray, rst9: np.ndarray,
+                  nJ: np.ndarray, J: np.ndarray, h: float = 0.0) -> TetMesh:
+    """A TetMesh from StartUpDG MeshData-shaped arrays (0-based): rd.Fmask (4*Nfp), md.mapP
+    (K*4*Nfp, element-major), per-element metric terms (K, 9) in the order rxJ, sxJ, txJ,
+    ryJ, syJ, tyJ, rzJ, szJ, tzJ, face-constant scaled normals (K, 4, 3) and J (K). The
+    connectivity and geometry records are built by the library (bb_conn_from_mapP,
+    bb_geo_from_meshdata); vertex arrays are not needed by the solver and are left empty."""
+    import ctypes
+    from . import _lib
+    K = int(np.asarray(J).shape[0])
+    fm = np.ascontiguousarray(Fmask, dtype=np.int32)
+    mp = np.ascontiguousarray(mapP, dtype=np.int64).reshape(-1)
+    conn = np.empty(K * 4, dtype=np.int32)
+    L = _lib.load(build_if_missing=True)
+    rc = L.bb_conn_from_mapP(int(N), K, fm.ctypes.data_as(ctypes.c_void_p),
+                             mp.ctypes.data_as(ctypes.c_void_p),
+                             conn.ctypes.data_as(ctypes.c_void_p))
+    if rc != 0:
+        raise ValueError("mapP does not describe a conforming face pairing")
+    r9 = np.ascontiguousarray(rst9, dtype=np.float64)
+    n3 = np.ascontiguousarray(nJ, dtype=np.float64)
+    jj = np.ascontiguousarray(J, dtype=np.float64)
+    geo = np.empty((K, GEO_STRIDE), dtype=np.float64)
+    rc = L.bb_geo_from_meshdata(K, _lib.BB_F64, r9.ctypes.data_as(ctypes.c_void_p),
+                                n3.ctypes.data_as(ctypes.c_void_p),
+                                jj.ctypes.data_as(ctypes.c_void_p),
+                                geo.ctypes.data_as(ctypes.c_void_p))
+    if rc != 0:
+        raise ValueError("bad geometry arrays")
+    c64 = conn.astype(np.int64).reshape(K, 4)
+    nbr, nbr_face, orient = c64 >> 5, (c64 >> 3) & 3, c64 & 7
+    return TetMesh(n=0, K=K, h=h, EVI=np.zeros((K, 4, 3), np.int64),
+                   EVX=np.zeros((K, 4, 3)), nbr=nbr, nbr_face=nbr_face, orient=orient,
+                   conn=conn.reshape(K, 4), geo=geo)

@@ -137,6 +137,19 @@ int bb_lsrk_run_host(bb_solver* s, double dt, int nsteps, const void* q_host_in,
                      void* q_host_out, void* q_dev, void* res_dev, int use_graph,
                      void* stream);
 
+/* ---- StartUpDG MeshData import (host functions, no device work) -------------------------
+ * conn_out[e*4+f] (the packed connectivity of bb_solver_create) from StartUpDG's
+ * rd.Fmask (4*Nfp volume indices, faces in reference order) and md.mapP (K*4*Nfp global
+ * face-node indices, element-major), both 0-based. Returns BB_ERR_ARG if a face side's nodes
+ * do not all meet one partner face through one of the six face symmetries. */
+int bb_conn_from_mapP(int N, int64_t K, const int32_t* Fmask, const int64_t* mapP,
+                      int32_t* conn_out);
+/* The geometry records of bb_solver_create (dtype BB_F32 or BB_F64, K*BB_GEO_STRIDE) from
+ * per-element affine metric terms rst9[e*9 + m] = (rxJ, sxJ, txJ, ryJ, syJ, tyJ, rzJ, szJ,
+ * tzJ)[m], face-constant scaled normals nJ[(e*4 + f)*3 + c] = (nxJ, nyJ, nzJ)[c] and J[e]. */
+int bb_geo_from_meshdata(int64_t K, int dtype, const double* rst9, const double* nJ,
+                         const double* J, void* geo_out);
+
 /* ---- degree reduction --------------------------------------------------------------
  * FP64 L2 projection of degree-N Bernstein coefficients to degree M < N, per element and
  * field: c_M = M_MM^{-1} E_{M->N}^T M_NN c_N (Bernstein mass matrices of the reference

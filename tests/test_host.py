@@ -117,3 +117,30 @@ def test_config4_problem_set_is_seeded_and_in_range():
     assert len(a) == 48 and a == b
     assert all(4 <= s.N <= 11 and 4 <= s.n <= 20 for s in a)
     assert {s.physics for s in a} == {"wave", "maxwell"}
+
+
+@pytest.mark.parametrize("N", [1, 2, 4, 7])
+def test_meshdata_import_rebuilds_connectivity_and_geometry(bb, N):
+    """bb_conn_from_mapP / bb_geo_from_meshdata on StartUpDG-shaped arrays (the oracle's
+    coordinate-matched mapP and cofactor geometry) reproduce the mesh's own records."""
+    from bbdg.mesh import from_meshdata
+    from oracle import meshdata
+    m = bb.uniform_tet_mesh(3)
+    md = meshdata.build(m, N)
+    Nfp = bb.np2(N)
+    nJ = md.nJ.reshape(m.K, 4, Nfp, 3)[:, :, 0, :]     # face-constant on affine faces
+    got = from_meshdata(N, md.Fmask, md.mapP, md.geo9, nJ, md.Jall, h=m.h)
+    assert np.array_equal(got.conn, m.conn)
+    assert np.allclose(got.geo, m.geo, rtol=1e-13, atol=1e-13)
+
+
+def test_meshdata_import_rejects_a_broken_mapP(bb):
+    from bbdg.mesh import from_meshdata
+    from oracle import meshdata
+    m = bb.uniform_tet_mesh(2)
+    md = meshdata.build(m, 2)
+    bad = md.mapP.copy()
+    bad[0], bad[1] = bad[1], bad[0] + 3 * bb.np2(2)    # two nodes of one face to different faces
+    nJ = md.nJ.reshape(m.K, 4, bb.np2(2), 3)[:, :, 0, :]
+    with pytest.raises(ValueError):
+        from_meshdata(2, md.Fmask, bad, md.geo9, nJ, md.Jall)
