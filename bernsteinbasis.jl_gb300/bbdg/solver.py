@@ -111,6 +111,13 @@ class DGSolver:
                        "bb_rhs")
         return out
 
+    def ode_rhs(self):
+        """f(t, q) -> dq/dt for external integrators (the OrdinaryDiffEq `rhs_matvec!(du, u,
+        params, t)` role): one bb_rhs per call on a device state, t unused (autonomous)."""
+        def f(t, q):
+            return self.rhs(q)
+        return f
+
     def run(self, q: torch.Tensor, res: torch.Tensor, dt: float, nsteps: int,
             graph: bool = True, stream=None) -> None:
         """Advance q (and the LSRK register res) by nsteps steps in place."""

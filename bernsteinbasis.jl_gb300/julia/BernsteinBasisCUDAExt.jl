@@ -115,6 +115,14 @@ function bernstein_rhs!(du::CuArray{T,3}, q::CuArray{T,3}, s::BBSolver{T}) where
     return du
 end
 
+# OrdinaryDiffEq interop: the examples' `rhs_matvec!(du, u, params, t)` signature with the
+# solver as `params`, so any integrator drives the GPU right-hand side on a CuArray state:
+#     prob = ODEProblem(gpu_rhs!, to_device_state(modal_u0), tspan, s)
+#     sol  = solve(prob, Tsit5(), dt = 0.01)          # examples/3d_wave.jl:133-134
+# (The solver's own fused LSRK45 loop, `lsrk_run!`, avoids the integrator's extra passes.)
+gpu_rhs!(du::CuArray{T,3}, u::CuArray{T,3}, s::BBSolver{T}, t) where {T} =
+    (bernstein_rhs!(du, u, s); nothing)
+
 function lsrk_run!(q::CuArray{T,3}, res::CuArray{T,3}, s::BBSolver{T}, dt::Real, nsteps::Integer;
                    graph::Bool = true) where {T}
     check(ccall((:bb_lsrk_run, libbbdg), Cint,
@@ -129,6 +137,6 @@ to_device_state(q::AbstractMatrix{<:AbstractVector{T}}) where {T} =
 from_device_state(q::CuArray{T,3}, ::Val{nf}) where {T,nf} =
     map(v -> SVector{nf,T}(v), eachslice(permutedims(Array(q), (3, 1, 2)); dims = (2, 3)))
 
-export bernstein_rhs!, lsrk_run!, BBSolver, to_device_state, from_device_state
+export bernstein_rhs!, gpu_rhs!, lsrk_run!, BBSolver, to_device_state, from_device_state
 
 end # module

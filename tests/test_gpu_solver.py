@@ -305,3 +305,31 @@ def test_advection_example_end_check(cuda, bb, oracle_cpu, dt):
     u = np.einsum("pn,kn->kp", V, got[0].astype(np.float64))
     ex = np.sin(np.pi * (x - T)) * np.sin(np.pi * y) * np.sin(np.pi * z)
     assert np.abs(u - ex).max() < 1e-3
+
+
+def test_external_integrator_drives_the_rhs(cuda, bb, oracle_cpu):
+    """An integrator outside the library (classical RK4 written here) through
+    DGSolver.ode_rhs(), the OrdinaryDiffEq interop path, against the same RK4 loop on the
+    oracle's right-hand side (FP64, 1e-12 per field)."""
+    import torch
+    m = bb.uniform_tet_mesh(3)
+    N = 4
+    md = meshdata.build(m, N)
+    s = bb.DGSolver(m, N, "wave", dtype=torch.float64, tau=1.0)
+    q0 = bb.project_fields(m, N, pulse_fields(4))
+    dt, nsteps = s.dt_cfl(), 6
+
+    def rk4(f, q):
+        for i in range(nsteps):
+            t = i * dt
+            k1 = f(t, q)
+            k2 = f(t + dt / 2, q + dt / 2 * k1)
+            k3 = f(t + dt / 2, q + dt / 2 * k2)
+            k4 = f(t + dt, q + dt * k3)
+            q = q + dt / 6 * (k1 + 2 * k2 + 2 * k3 + k4)
+        return q
+
+    got = rk4(s.ode_rhs(), torch.tensor(q0, device=cuda)).cpu().numpy()
+    want = rk4(lambda t, q: oracle_cpu.rhs(0, N, q, md, tau=1.0), np.asarray(q0))
+    err = per_field_rel(got, want)
+    assert np.all(err < 1e-12), err
