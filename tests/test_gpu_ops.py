@@ -67,6 +67,33 @@ def test_lift_matches_oracle(cuda, bb, oracle_cpu, N, dt, K):
     assert rel(of.cpu().numpy(), want) < TOL[dt]
 
 
+@pytest.mark.parametrize("N", [3, 9, 10, 12])
+def test_lift_fp32_many_tiles_and_misaligned(cuda, bb, oracle_cpu, N):
+    """K = 20011 gives more 8-element tiles than the grid has blocks, so every block works
+    through several tiles (the register-prefetch path for N <= 9, the bulk-copy path above)
+    and ends on a ragged one; a sample of columns is checked against the oracle. Inputs and
+    outputs that are not 16-byte aligned take the generic kernel and agree with it."""
+    import torch
+    rng = np.random.default_rng(90 + N)
+    K = 20011
+    Np, Nfp = bb.np3(N), bb.np2(N)
+    x = rng.uniform(-1, 1, (K, 4 * Nfp)).astype(np.float32)
+    xd = torch.tensor(x, device=cuda)
+    out = torch.empty((K, Np), dtype=torch.float32, device=cuda)
+    bb.mul_(out, bb.BernsteinLift(N), xd)
+    cols = np.r_[0:40, K // 2:K // 2 + 40, K - 40:K]
+    want = oracle_cpu.lift(N, x[cols].astype(np.float64))
+    assert rel(out.cpu().numpy()[cols], want) < TOL["f32"]
+    # misaligned views (offset by one float) run the generic kernel
+    Km = 300
+    xb = torch.tensor(np.concatenate([[0.0], x[:Km].ravel()]).astype(np.float32), device=cuda)
+    ob = torch.empty(Km * Np + 1, dtype=torch.float32, device=cuda)
+    xm, om = xb[1:].view(Km, 4 * Nfp), ob[1:].view(Km, Np)
+    assert xm.data_ptr() % 16 != 0
+    bb.mul_(om, bb.BernsteinLift(N), xm)
+    assert rel(om.cpu().numpy(), out[:Km].cpu().numpy()) < TOL["f32"]
+
+
 @pytest.mark.parametrize("dt", ["f64", "f32"])
 @pytest.mark.parametrize("N", [1, 2, 5, 9, 14, 19])
 def test_elevation_reduction_match_oracle(cuda, bb, oracle_cpu, N, dt):
