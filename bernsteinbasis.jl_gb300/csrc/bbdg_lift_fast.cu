@@ -31,29 +31,15 @@ __host__ __device__ constexpr int lf_ijk(int n, int i, int j, int k) {
   return i + lf_tri(n, j) + lf_tet(n, k) - j * k;
 }
 
-// l_d(N) of src/constants.jl:10-12, evaluated at compile time (same double arithmetic as the
-// host tables, rounded once to float).
-__host__ __device__ constexpr double lf_lj(int N, int d) {
-  double b = 1.0;
-  for (int m = 1; m <= d; ++m) b = b * (N - d + m) / m;
-  return ((d % 2) ? -1.0 : 1.0) * b / (1.0 + d);
-}
-template <int N>
-struct LiftWeights {
-  float v[N + 1];
-  __host__ __device__ constexpr LiftWeights() : v() {
-    v[0] = 1.0f;
-    for (int d = 1; d <= N; ++d) v[d] = (float)lf_lj(N, d);
-  }
-};
-
 // One face chain from the Nfp inputs X (registers) to the l_d-scaled stack g (shared memory,
-// g[lf_ijk(N, i, j, d)] = l_d E_d(i, j); for the t = -1 face this is the volume order).
+// g[lf_ijk(N, i, j, d)] = F_d(i, j) = l_d E_d(i, j); for the t = -1 face this is the volume
+// order). The chain carries F_d itself: l_d / l_{d-1} = -(N-d+1)/(d+1) and R_{N-d+1} divides by
+// N-d+1, so F_d = -1/(d+1) [(i+1) F_{d-1}(i+1,j) + (j+1) F_{d-1}(i,j+1) + (N-d+1-i-j) F_{d-1}(i,j)]
+// with F_0 = E_0 = L0 x.
 template <int N>
 __device__ __forceinline__ void lift_chain_stack(const float (&X)[(N + 1) * (N + 2) / 2],
                                                  float* g) {
   constexpr int NFP = (N + 1) * (N + 2) / 2;
-  constexpr LiftWeights<N> lw;
   float E[NFP];
 #pragma unroll
   for (int j = 0; j <= N; ++j) {
@@ -74,17 +60,18 @@ __device__ __forceinline__ void lift_chain_stack(const float (&X)[(N + 1) * (N +
 #pragma unroll
   for (int d = 1; d <= N; ++d) {
     const int n = N - d + 1;  // input degree of this reduction
-    const float inv = 1.0f / float(n);
+    const float inv = -1.0f / float(d + 1);
 #pragma unroll
     for (int j = 0; j < n; ++j) {
 #pragma unroll
       for (int i = 0; i + j < n; ++i) {
-        // reduction_multiply! (src/BernsteinLift.jl:81-85), in place, ascending
+        // reduction_multiply! (src/BernsteinLift.jl:81-85) times l_d / l_{d-1}, in place,
+        // ascending
         const float v = float(i + 1) * inv * E[lf_ij(N, i + 1, j)] +
                         (float(j + 1) * inv * E[lf_ij(N, i, j + 1)] +
                          float(n - i - j) * inv * E[lf_ij(N, i, j)]);
         E[lf_ij(N, i, j)] = v;
-        g[lf_ijk(N, i, j, d)] = lw.v[d] * v;
+        g[lf_ijk(N, i, j, d)] = v;
       }
     }
   }

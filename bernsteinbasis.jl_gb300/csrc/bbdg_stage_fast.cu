@@ -42,13 +42,6 @@ __host__ __device__ constexpr int c_ij(int n, int i, int j) { return i + c_tri(n
 __host__ __device__ constexpr int c_ijk(int n, int i, int j, int k) {
   return i + c_tri(n, j) + c_tet(n, k) - j * k;
 }
-// l_j(N) of src/constants.jl:10-12
-__host__ __device__ inline float lift_lj(int N, int d) {
-  double b = 1.0;
-  for (int m = 1; m <= d; ++m) b = b * (N - d + m) / m;
-  return float(((d % 2) ? -1.0 : 1.0) * b / (1.0 + d));
-}
-
 template <int PHYS>
 struct FPhys;
 template <>
@@ -70,8 +63,10 @@ struct FastLayout {
   static constexpr int CHT = (NCHAIN + 31) / 32 * 32;  // chain threads, whole warps
   static constexpr int NTE = EPB * TPE;                // element threads
   static constexpr int NT = NTE + CHT;
-  static constexpr int NPS = NP | 1;  // chain stack stride: odd, so same-offset accesses of
-                                      // the chain threads fall in different banks
+  // chain stacks: element-face e4 = element * 4 + face holds its NCH chains interleaved,
+  // entry (e4, p, ch) at (e4 * NPS + p) * NCH + ch. NPS = 1 mod 16 puts the same entry of the
+  // 32 chains of a warp (consecutive e4 and ch) in 32 different banks for NCH = 2 and 6.
+  static constexpr int NPS = (NP + 14) / 16 * 16 + 1;
   static constexpr int NPM1P = NPM1 + 1;  // volume rows end with a zero entry (index NPM1)
   // bytes; every bulk-copy destination starts on a 16-byte boundary
   static constexpr int QBYTES = NF * EPB * NP * 4;            // q tile, [NF][EPB][NP]
@@ -79,13 +74,12 @@ struct FastLayout {
   static constexpr int CONNBYTES = EPB * 16;                   // [EPB][4] int32
   static constexpr int SLOT = ((QBYTES + GEOBYTES + CONNBYTES) + 15) / 16 * 16;
   static constexpr int RES_B = 2 * SLOT;                       // after the two q slots
-  static constexpr int G_B = RES_B + QBYTES;                   // [NCHAIN][NPS] face stacks
+  static constexpr int G_B = RES_B + QBYTES;                   // [EPB*4][NPS][NCH] face stacks
   static constexpr int X_B = G_B + (NCHAIN * NPS * 4 + 15) / 16 * 16;  // [2][NCHAIN][NFP]
-  static constexpr int W_B = X_B + (2 * NCHAIN * NFP * 4 + 15) / 16 * 16;  // [NW][EPB][NPM1P]
+  static constexpr int W_B = X_B + (2 * NCHAIN * NFP * 4 + 15) / 16 * 16;  // [EPB][NPM1P][NW]
   static constexpr int GA_B = W_B + (NW * EPB * NPM1P * 4 + 15) / 16 * 16;  // [NP] uint4
   static constexpr int GW_B = GA_B + NP * 16;                  // [NP] float4 alpha_b
-  static constexpr int LW_B = GW_B + NP * 16;                  // [NP] float4 l_d per face
-  static constexpr int VN_B = LW_B + NP * 16;                  // [NPM1] uint2
+  static constexpr int VN_B = GW_B + NP * 16;                  // [NPM1] uint2
   static constexpr int FVOL_B = VN_B + NPM1 * 8;               // [4][NFP] u16
   static constexpr int FPERM_B = FVOL_B + ((4 * NFP * 2 + 3) / 4 * 4);  // [6][NFP] u16
   static constexpr int FNB_B = FPERM_B + ((6 * NFP * 2 + 3) / 4 * 4);  // [4][6][NFP] u16
@@ -162,9 +156,11 @@ __device__ __forceinline__ void named_sync(int id, int count) {
 }
 
 // One face lift chain for compile-time N: x = chain input (NFP values, smem); g = the face's
-// volume stack, g[c_ijk(N,i,j,d)] = E_d(i,j) (unscaled; the l_d factors are applied when the
-// stacks are summed). All of x is read before g is written.
-template <int N>
+// volume stack with entries NCH apart, g[c_ijk(N,i,j,d) * NCH] = F_d(i,j) = l_d E_d(i,j). The
+// chain carries F_d itself: l_d / l_{d-1} = -(N-d+1)/(d+1) and R_{N-d+1} divides by N-d+1, so
+// F_d = -1/(d+1) [(i+1) F_{d-1}(i+1,j) + (j+1) F_{d-1}(i,j+1) + (N-d+1-i-j) F_{d-1}(i,j)]
+// (F_0 = E_0 = L0 x). All of x is read before g is written.
+template <int N, int NCH>
 __device__ __forceinline__ void lift_chain(const float* x, float* g) {
   constexpr int NFP = (N + 1) * (N + 2) / 2;
   float X[NFP];
@@ -187,21 +183,22 @@ __device__ __forceinline__ void lift_chain(const float* x, float* g) {
     }
   }
 #pragma unroll
-  for (int m = 0; m < NFP; ++m) g[m] = E[m];  // layer 0 (c_ijk(N,i,j,0) = c_ij(N,i,j))
+  for (int m = 0; m < NFP; ++m) g[m * NCH] = E[m];  // layer 0 (c_ijk(N,i,j,0) = c_ij(N,i,j))
 #pragma unroll
   for (int d = 1; d <= N; ++d) {
     const int n = N - d + 1;  // input degree; E indexed with the degree-N layout
-    const float inv = 1.0f / float(n);
+    const float inv = -1.0f / float(d + 1);
 #pragma unroll
     for (int j = 0; j < n; ++j) {
 #pragma unroll
       for (int i = 0; i + j < n; ++i) {
-        // reduction_multiply! (src/BernsteinLift.jl:81-85), in place in ascending order
+        // reduction_multiply! (src/BernsteinLift.jl:81-85) times l_d / l_{d-1}, in place in
+        // ascending order
         const float v = float(i + 1) * inv * E[c_ij(N, i + 1, j)] +
                         (float(j + 1) * inv * E[c_ij(N, i, j + 1)] +
                          float(n - i - j) * inv * E[c_ij(N, i, j)]);
         E[c_ij(N, i, j)] = v;
-        g[c_ijk(N, i, j, d)] = v;
+        g[c_ijk(N, i, j, d) * NCH] = v;
       }
     }
   }
@@ -227,7 +224,6 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
   // alpha_b = 0) and face-stack positions; alpha_b; l_d of its layer on each face
   uint4* sGA = reinterpret_cast<uint4*>(smem + L::GA_B);
   float4* sGW = reinterpret_cast<float4*>(smem + L::GW_B);
-  float4* sLW = reinterpret_cast<float4*>(smem + L::LW_B);
   uint2* sVN = reinterpret_cast<uint2*>(smem + L::VN_B);  // beta -> indices of beta + e_a
   uint16_t* sFvol = reinterpret_cast<uint16_t*>(smem + L::FVOL_B);
   uint16_t* sFperm = reinterpret_cast<uint16_t*>(smem + L::FPERM_B);
@@ -295,10 +291,6 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
       const uint32_t p0 = ijk3(N, i, k, j), p1 = ijk3(N, j, k, l), p2 = ijk3(N, j, k, i);
       sGA[t] = make_uint4(m0 | (m1 << 16), m2 | (m3 << 16), 0u, p0 | (p1 << 10) | (p2 << 20));
       sGW[t] = make_float4(float(i), float(j), float(k), float(l));
-      // l_d of the layer this coefficient sits in on faces f0..f3 (distances j, l, i, k);
-      // layer 0 carries the L0 block itself (weight 1)
-      auto lw = [](int d) { return d == 0 ? 1.0f : lift_lj(N, d); };
-      sLW[t] = make_float4(lw(j), lw(l), lw(i), lw(k));
       // face nodes: f0 (j=0) at (i,k), f1 (l=0) at (j,k), f2 (i=0) at (j,k), f3 (k=0) at (i,j)
       const uint32_t a0 = j == 0 ? (uint32_t)ij2(N, i, k) : 0xffu;
       const uint32_t a1 = l == 0 ? (uint32_t)ij2(N, j, k) : 0xffu;
@@ -312,7 +304,7 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
       sVN[t] = make_uint2(ijk3(N, i + 1, j, k) | (ijk3(N, i, j + 1, k) << 16),
                           ijk3(N, i, j, k + 1) | (ijk3(N, i, j, k) << 16));
     }
-    for (int t = tid; t < NW * EPB; t += NT) sW[t * L::NPM1P + NPM1] = 0.f;
+    for (int t = tid; t < NW * EPB; t += NT) sW[((t / NW) * L::NPM1P + NPM1) * NW + t % NW] = 0.f;
     const uint16_t* gf = reinterpret_cast<const uint16_t*>(gw + P.o_fvol);
     for (int t = tid; t < 4 * NFP; t += NT) sFvol[t] = gf[t];
     const uint16_t* gp = reinterpret_cast<const uint16_t*>(gw + P.o_fperm);
@@ -430,7 +422,7 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
     //         this tile, then the interface flux of the next tile -------------------------
     if (!is_elem) {
       const int c = tid - NTE;
-      if (c < NCHAIN) lift_chain<N>(sX + (s * NCHAIN + c) * NFP, sG + c * NPS);
+      if (c < NCHAIN) lift_chain<N, NCH>(sX + (s * NCHAIN + c) * NFP, sG + (c / NCH) * NPS * NCH + c % NCH);
     } else {
       // the tile after next: its outside-tile neighbour traces (one contiguous NF x Nfp block
       // per face) are pulled into L2 now, a whole tile ahead of its flux phase
@@ -487,8 +479,13 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
             w[5] += gx[a] * Hy - gy[a] * Hx;
           }
         }
+        float* wd = sW + (le * L::NPM1P + b) * NW;
+        if constexpr (NW == 4) {
+          *reinterpret_cast<float4*>(wd) = make_float4(w[0], w[1], w[2], w[3]);
+        } else {
 #pragma unroll
-        for (int m = 0; m < NW; ++m) sW[(m * EPB + le) * L::NPM1P + b] = w[m];
+          for (int m = 0; m < NW; m += 2) *reinterpret_cast<float2*>(wd + m) = make_float2(w[m], w[m + 1]);
+        }
       }
       if (pre) {
         const int64_t nb = (int64_t)((uint32_t)cpre >> 5);
@@ -528,8 +525,8 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
         nyf[f] = g[16 + f];
         nzf[f] = g[20 + f];
       }
-      const float* G = sG + le * 4 * NCH * NPS;
-      const float* wb = sW + le * L::NPM1P;
+      const float* G = sG + le * 4 * NPS * NCH;   // this element's four face stacks
+      const float* wb = sW + le * L::NPM1P * NW;  // this element's w(beta), NW per point
       // faces whose partner lies outside this tile need their updated trace in HBM
       bool leave[4];
 #pragma unroll
@@ -546,42 +543,81 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
         if (n >= NP) continue;
         const uint4 ga = sGA[n];
         const float4 gw4 = sGW[n];
-        const float4 lw = sLW[n];
-        const float lwf[4] = {lw.x, lw.y, lw.z, lw.w};
         const int p[4] = {(int)(ga.w & 1023), (int)((ga.w >> 10) & 1023), (int)(ga.w >> 20), n};
-        const int x0 = ga.x & 0xffff, x1 = ga.x >> 16, x2 = ga.y & 0xffff, x3 = ga.y >> 16;
+        const int xb[4] = {(int)(ga.x & 0xffff), (int)(ga.x >> 16), (int)(ga.y & 0xffff),
+                           (int)(ga.y >> 16)};
+        const float ab[4] = {gw4.x, gw4.y, gw4.z, gw4.w};
+        // vol(alpha) = sum_b alpha_b w(alpha - e_b), b = 3 first (as the fma nesting before)
         float vol[NW];
+        if constexpr (NW == 4) {
+          const float4 w3 = *reinterpret_cast<const float4*>(wb + xb[3] * 4);
+          vol[0] = ab[3] * w3.x;
+          vol[1] = ab[3] * w3.y;
+          vol[2] = ab[3] * w3.z;
+          vol[3] = ab[3] * w3.w;
 #pragma unroll
-        for (int m = 0; m < NW; ++m) {
-          const float* wm = wb + m * EPB * L::NPM1P;
-          vol[m] = fmaf(gw4.x, wm[x0], fmaf(gw4.y, wm[x1], fmaf(gw4.z, wm[x2], gw4.w * wm[x3])));
+          for (int b = 2; b >= 0; --b) {
+            const float4 wv = *reinterpret_cast<const float4*>(wb + xb[b] * 4);
+            vol[0] = fmaf(ab[b], wv.x, vol[0]);
+            vol[1] = fmaf(ab[b], wv.y, vol[1]);
+            vol[2] = fmaf(ab[b], wv.z, vol[2]);
+            vol[3] = fmaf(ab[b], wv.w, vol[3]);
+          }
+        } else {
+#pragma unroll
+          for (int m = 0; m < NW; m += 2) {
+            const float2 w3 = *reinterpret_cast<const float2*>(wb + xb[3] * NW + m);
+            vol[m] = ab[3] * w3.x;
+            vol[m + 1] = ab[3] * w3.y;
+          }
+#pragma unroll
+          for (int b = 2; b >= 0; --b) {
+#pragma unroll
+            for (int m = 0; m < NW; m += 2) {
+              const float2 wv = *reinterpret_cast<const float2*>(wb + xb[b] * NW + m);
+              vol[m] = fmaf(ab[b], wv.x, vol[m]);
+              vol[m + 1] = fmaf(ab[b], wv.y, vol[m + 1]);
+            }
+          }
         }
         float* rhs = rhs_all[r];
         if constexpr (PHYS == BB_WAVE) {
-          // face order of src/BernsteinLift.jl:202-214: t=-1 face first, then f1, f2, f3
-          const float B3 = lwf[3] * G[(3 * 2 + 1) * NPS + p[3]];
-          float A = lwf[3] * G[(3 * 2 + 0) * NPS + p[3]];
-          float Bx = nxf[3] * B3, By = nyf[3] * B3, Bz = nzf[3] * B3;
+          // face order of src/BernsteinLift.jl:202-214: t=-1 face first, then f1, f2, f3;
+          // the stacks already carry the l_d weights
+          const float2 g3 = *reinterpret_cast<const float2*>(G + (3 * NPS + p[3]) * 2);
+          float A = g3.x;
+          float Bx = nxf[3] * g3.y, By = nyf[3] * g3.y, Bz = nzf[3] * g3.y;
 #pragma unroll
           for (int f = 0; f < 3; ++f) {
-            const float Bf = lwf[f] * G[(f * 2 + 1) * NPS + p[f]];
-            A = fmaf(lwf[f], G[(f * 2 + 0) * NPS + p[f]], A);
-            Bx = fmaf(nxf[f], Bf, Bx);
-            By = fmaf(nyf[f], Bf, By);
-            Bz = fmaf(nzf[f], Bf, Bz);
+            const float2 gf = *reinterpret_cast<const float2*>(G + (f * NPS + p[f]) * 2);
+            A += gf.x;
+            Bx = fmaf(nxf[f], gf.y, Bx);
+            By = fmaf(nyf[f], gf.y, By);
+            Bz = fmaf(nzf[f], gf.y, Bz);
           }
           rhs[0] = (A - vol[0]) * invJ;
           rhs[1] = (Bx - vol[1]) * invJ;
           rhs[2] = (By - vol[2]) * invJ;
           rhs[3] = (Bz - vol[3]) * invJ;
         } else {
+          float v[6];
 #pragma unroll
-          for (int m = 0; m < 6; ++m) {
-            float v = lwf[3] * G[(3 * 6 + m) * NPS + p[3]];
-#pragma unroll
-            for (int f = 0; f < 3; ++f) v = fmaf(lwf[f], G[(f * 6 + m) * NPS + p[f]], v);
-            rhs[m] = (v + vol[m]) * invJ;
+          for (int m = 0; m < 6; m += 2) {
+            const float2 g3 = *reinterpret_cast<const float2*>(G + (3 * NPS + p[3]) * 6 + m);
+            v[m] = g3.x;
+            v[m + 1] = g3.y;
           }
+#pragma unroll
+          for (int f = 0; f < 3; ++f) {
+#pragma unroll
+            for (int m = 0; m < 6; m += 2) {
+              const float2 gf = *reinterpret_cast<const float2*>(G + (f * NPS + p[f]) * 6 + m);
+              v[m] += gf.x;
+              v[m + 1] += gf.y;
+            }
+          }
+#pragma unroll
+          for (int m = 0; m < 6; ++m) rhs[m] = (v[m] + vol[m]) * invJ;
         }
       }
       float* __restrict__ gq_out = P.q;
