@@ -67,7 +67,13 @@ struct FastLayout {
   // entry (e4, p, ch) at (e4 * NPS + p) * NCH + ch. NPS = 1 mod 16 puts the same entry of the
   // 32 chains of a warp (consecutive e4 and ch) in 32 different banks for NCH = 2 and 6.
   static constexpr int NPS = (NP + 14) / 16 * 16 + 1;
-  static constexpr int NPM1P = NPM1 + 1;  // volume rows end with a zero entry (index NPM1)
+  // w(beta) rows: NPM1 entries, then NZ zero entries from Z0 (a multiple of 8) on, one per bank
+  // group of the gather's vector loads (16-byte entries: 8 lanes per phase, 8 groups; 24-byte
+  // entries: 16 lanes per phase, bank pair 3 x mod 16); a coefficient with alpha_b = 0 reads the
+  // zero entry whose group no other lane of its phase reads, so the zero never conflicts
+  static constexpr int Z0 = (NPM1 + 7) / 8 * 8;
+  static constexpr int NZ = NW == 4 ? 8 : 16;
+  static constexpr int NPM1P = Z0 + NZ;
   // bytes; every bulk-copy destination starts on a 16-byte boundary
   static constexpr int QBYTES = NF * EPB * NP * 4;            // q tile, [NF][EPB][NP]
   static constexpr int GEOBYTES = EPB * BB_GEO_STRIDE * 4;     // [EPB][24]
@@ -211,6 +217,7 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
   using L = FastLayout<N, PHYS, EPB, TPE>;
   constexpr int NP = L::NP, NFP = L::NFP, NPM1 = L::NPM1, NF = L::NF, NCH = L::NCH;
   constexpr int NPS = L::NPS, NCHAIN = L::NCHAIN, NW = L::NW, NTE = L::NTE, NT = L::NT;
+  constexpr int NZ_W = EPB * L::NZ * NW;  // zero-entry floats of all elements
   constexpr int FT = TPE / 4;                     // element threads per face
   constexpr int FR = (NFP + FT - 1) / FT;         // face nodes per element thread
   constexpr int VR = (NPM1 + TPE - 1) / TPE;      // degree N-1 points per element thread
@@ -279,14 +286,40 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
   // constant tables (built from the degree tables in global memory)
   {
     const uint32_t* gw = P.gtab;
-    constexpr uint32_t Z = NPM1;
+    // w index of alpha - e_b, or -1 when alpha_b = 0
+    auto wnb = [&](int n, int b) {
+      const uint32_t c = gw[P.o_node3 + n];
+      const int i = c & 0xff, j = (c >> 8) & 0xff, k = c >> 16, l = N - i - j - k;
+      const int ab = b == 0 ? i : b == 1 ? j : b == 2 ? k : l;
+      if (ab == 0) return -1;
+      return ijk3(N - 1, i - (b == 0), j - (b == 1), k - (b == 2));
+    };
+    auto group_of = [](int x) { return NW == 4 ? (x & 7) : ((3 * x) & 15); };
     for (int t = tid; t < NP; t += NT) {
       const uint32_t c = gw[P.o_node3 + t];
       const int i = c & 0xff, j = (c >> 8) & 0xff, k = c >> 16, l = N - i - j - k;
-      const uint32_t m0 = i > 0 ? ijk3(N - 1, i - 1, j, k) : Z;
-      const uint32_t m1 = j > 0 ? ijk3(N - 1, i, j - 1, k) : Z;
-      const uint32_t m2 = k > 0 ? ijk3(N - 1, i, j, k - 1) : Z;
-      const uint32_t m3 = l > 0 ? ijk3(N - 1, i, j, k) : Z;
+      uint32_t mb[4];
+      const int lane = (t % TPE) & 31, phase = L::NZ;  // lanes of one vector-load phase
+      const int n0 = t - (lane % phase);
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        const int x = wnb(t, b);
+        if (x >= 0) {
+          mb[b] = (uint32_t)x;
+          continue;
+        }
+        uint32_t used = 0;
+        for (int q = 0; q < phase; ++q) {
+          const int nq = n0 + q;
+          if (nq >= NP || (nq % TPE) / 32 != (t % TPE) / 32) continue;
+          const int xq = wnb(nq, b);
+          if (xq >= 0) used |= 1u << group_of(xq);
+        }
+        int zs = 0;
+        while (zs < L::NZ - 1 && ((used >> group_of(L::Z0 + zs)) & 1u)) ++zs;
+        mb[b] = (uint32_t)(L::Z0 + zs);
+      }
+      const uint32_t m0 = mb[0], m1 = mb[1], m2 = mb[2], m3 = mb[3];
       // stack positions of this coefficient on faces f0 (i,k,j), f1 (j,k,l), f2 (j,k,i)
       const uint32_t p0 = ijk3(N, i, k, j), p1 = ijk3(N, j, k, l), p2 = ijk3(N, j, k, i);
       sGA[t] = make_uint4(m0 | (m1 << 16), m2 | (m3 << 16), 0u, p0 | (p1 << 10) | (p2 << 20));
@@ -304,7 +337,8 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
       sVN[t] = make_uint2(ijk3(N, i + 1, j, k) | (ijk3(N, i, j + 1, k) << 16),
                           ijk3(N, i, j, k + 1) | (ijk3(N, i, j, k) << 16));
     }
-    for (int t = tid; t < NW * EPB; t += NT) sW[((t / NW) * L::NPM1P + NPM1) * NW + t % NW] = 0.f;
+    for (int t = tid; t < NZ_W; t += NT)
+      sW[((t / (L::NZ * NW)) * L::NPM1P + L::Z0 + (t / NW) % L::NZ) * NW + t % NW] = 0.f;
     const uint16_t* gf = reinterpret_cast<const uint16_t*>(gw + P.o_fvol);
     for (int t = tid; t < 4 * NFP; t += NT) sFvol[t] = gf[t];
     const uint16_t* gp = reinterpret_cast<const uint16_t*>(gw + P.o_fperm);
