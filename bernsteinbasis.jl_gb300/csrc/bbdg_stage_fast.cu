@@ -27,7 +27,10 @@
 // update, storing q, res and the outgoing face traces straight to HBM. q, geometry and
 // connectivity of tile i+2 and res of tile i+1 arrive by bulk copies (cp.async.bulk,
 // mbarrier completion, bounded waits) while tiles i and i+1 are being worked on.
+#include <algorithm>
+#include <array>
 #include <cmath>
+#include <vector>
 
 #include "bbdg_internal.cuh"
 #include "bbdg_stage_fast.cuh"
@@ -474,8 +477,9 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
       // w(beta) at degree N-1; vol(alpha) = sum_b alpha_b w(alpha - e_b) is formed in B
 #pragma unroll
       for (int r = 0; r < VR; ++r) {
-        const int b = u + r * TPE;
-        if (b >= NPM1) continue;
+        const int vg = r * (TPE / 32) + (u >> 5), lane = u & 31;
+        if (lane >= P.vlen[vg]) continue;
+        const int b = P.vstart[vg] + lane;
         const uint2 vn = sVN[b];
         const int idx[4] = {(int)(vn.x & 0xffff), (int)(vn.x >> 16), (int)(vn.y & 0xffff),
                             (int)(vn.y >> 16)};
@@ -710,10 +714,92 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
   if (tid == 0) tma_store_wait_all();
 }
 
+// Volume-phase work split (host, once per variant): the NPM1 points beta, in index order, are
+// cut into VR * TPE / 32 contiguous ranges of at most 32, one per warp-round, where the cuts
+// minimise the shared-memory wavefronts of the phase's accesses: the NF-field q reads at
+// beta + e_a (a = 0..3, 32 lanes, one word each) and the w(beta) store (NW floats per point, in
+// 16-byte or 8-byte pieces). Exact dynamic programme over the cut positions.
+struct VolGroups {
+  uint8_t start[16], len[16];
+};
+template <int N, int PHYS, int TPE>
+VolGroups volume_groups() {
+  constexpr int NPM1 = N * (N + 1) * (N + 2) / 6, NF = FPhys<PHYS>::NF, NW = FPhys<PHYS>::NW;
+  constexpr int VR = (NPM1 + TPE - 1) / TPE, G = VR * (TPE / 32);
+  static_assert(G <= 16 && NPM1 < 256, "volume groups fit the launch parameters");
+  std::vector<std::array<int, 4>> qi(NPM1);
+  for (int k = 0, b = 0; k < N; ++k)
+    for (int j = 0; j < N - k; ++j)
+      for (int i = 0; i < N - j - k; ++i, ++b)
+        qi[b] = {ijk3(N, i + 1, j, k), ijk3(N, i, j + 1, k), ijk3(N, i, j, k + 1), ijk3(N, i, j, k)};
+  // wavefronts of one access: per phase of `lanes` lanes, the largest number of distinct
+  // addresses (in units of `unit` words) that share a bank group
+  auto wavefronts = [](const std::vector<int>& words, int unit, int lanes) {
+    int tot = 0;
+    const int groups = 32 / unit;
+    for (size_t p0 = 0; p0 < words.size(); p0 += lanes) {
+      int best = 0;
+      for (int g = 0; g < groups; ++g) {
+        int cnt = 0;
+        std::vector<int> seen;
+        for (size_t q = p0; q < words.size() && q < p0 + lanes; ++q) {
+          const int a = words[q] / unit;
+          if (a % groups != g) continue;
+          bool dup = false;
+          for (int x : seen) dup |= x == a;
+          if (!dup) seen.push_back(a), ++cnt;
+        }
+        best = std::max(best, cnt);
+      }
+      tot += best;
+    }
+    return tot;
+  };
+  auto range_cost = [&](int a, int b) {
+    if (b <= a) return 0;
+    int c = 0;
+    std::vector<int> w;
+    for (int t = 0; t < 4; ++t) {
+      w.clear();
+      for (int x = a; x < b; ++x) w.push_back(qi[x][t]);
+      c += NF * wavefronts(w, 1, 32);
+    }
+    w.clear();
+    for (int x = a; x < b; ++x) w.push_back(x * NW);
+    c += NW == 4 ? wavefronts(w, 4, 8) : (NW / 2) * wavefronts(w, 2, 16);
+    return c;
+  };
+  std::vector<std::array<int, 33>> rc(NPM1 + 1);  // rc[a][n] = cost of [a, a + n)
+  for (int a = 0; a <= NPM1; ++a)
+    for (int n = 0; n <= 32; ++n) rc[a][n] = a + n <= NPM1 ? range_cost(a, a + n) : 0;
+  const int INF = 1 << 29;
+  std::vector<std::vector<int>> dp(G + 1, std::vector<int>(NPM1 + 1, INF)),
+      arg(G + 1, std::vector<int>(NPM1 + 1, 0));
+  dp[0][0] = 0;
+  for (int g = 1; g <= G; ++g)
+    for (int i = 0; i <= NPM1; ++i)
+      for (int a = std::max(0, i - 32); a <= i; ++a) {
+        if (dp[g - 1][a] >= INF) continue;
+        const int c = dp[g - 1][a] + rc[a][i - a];
+        if (c < dp[g][i]) dp[g][i] = c, arg[g][i] = a;
+      }
+  VolGroups v{};
+  for (int g = G, i = NPM1; g >= 1; --g) {
+    const int a = arg[g][i];
+    v.start[g - 1] = (uint8_t)a;
+    v.len[g - 1] = (uint8_t)(i - a);
+    i = a;
+  }
+  return v;
+}
+
 template <int N, int PHYS, int EPB, int TPE>
-int launch_fast_t(const FastLaunch& fl, const FastStageParams& P, cudaStream_t st) {
+int launch_fast_t(const FastLaunch& fl, const FastStageParams& P0, cudaStream_t st) {
   using L = FastLayout<N, PHYS, EPB, TPE>;
   auto kern = stage_fast_kernel<N, PHYS, EPB, TPE>;
+  static const VolGroups vg = volume_groups<N, PHYS, TPE>();
+  FastStageParams P = P0;
+  for (int g = 0; g < 16; ++g) P.vstart[g] = vg.start[g], P.vlen[g] = vg.len[g];
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES) !=
       cudaSuccess)
     return BB_ERR_CUDA;

@@ -17,6 +17,9 @@ struct FastStageParams {
   const float* geo;      // [K][BB_GEO_STRIDE]
   const int32_t* conn;   // [K][4]
   int* status;
+  // volume phase: warp-round g = r * (TPE / 32) + warp forms w(beta) for beta = vstart[g] +
+  // lane, lane < vlen[g] (filled by the launcher)
+  uint8_t vstart[16], vlen[16];
 };
 
 struct FastLaunch {
