@@ -87,8 +87,7 @@ struct FastLayout {
   static constexpr int X_B = G_B + (NCHAIN * NPS * 4 + 15) / 16 * 16;  // [2][NCHAIN][NFP]
   static constexpr int W_B = X_B + (2 * NCHAIN * NFP * 4 + 15) / 16 * 16;  // [EPB][NPM1P][NW]
   static constexpr int GA_B = W_B + (NW * EPB * NPM1P * 4 + 15) / 16 * 16;  // [NP] uint4
-  static constexpr int GW_B = GA_B + NP * 16;                  // [NP] float4 alpha_b
-  static constexpr int VN_B = GW_B + NP * 16;                  // [NPM1] uint2
+  static constexpr int VN_B = GA_B + NP * 16;                  // [NPM1] uint2
   static constexpr int FVOL_B = VN_B + NPM1 * 8;               // [4][NFP] u16
   static constexpr int FPERM_B = FVOL_B + ((4 * NFP * 2 + 3) / 4 * 4);  // [6][NFP] u16
   static constexpr int FNB_B = FPERM_B + ((6 * NFP * 2 + 3) / 4 * 4);  // [4][6][NFP] u16
@@ -233,7 +232,6 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
   // per coefficient alpha: degree N-1 indices of alpha - e_b (NPM1 = zero entry when
   // alpha_b = 0) and face-stack positions; alpha_b; l_d of its layer on each face
   uint4* sGA = reinterpret_cast<uint4*>(smem + L::GA_B);
-  float4* sGW = reinterpret_cast<float4*>(smem + L::GW_B);
   uint2* sVN = reinterpret_cast<uint2*>(smem + L::VN_B);  // beta -> indices of beta + e_a
   uint16_t* sFvol = reinterpret_cast<uint16_t*>(smem + L::FVOL_B);
   uint16_t* sFperm = reinterpret_cast<uint16_t*>(smem + L::FPERM_B);
@@ -325,8 +323,10 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
       const uint32_t m0 = mb[0], m1 = mb[1], m2 = mb[2], m3 = mb[3];
       // stack positions of this coefficient on faces f0 (i,k,j), f1 (j,k,l), f2 (j,k,i)
       const uint32_t p0 = ijk3(N, i, k, j), p1 = ijk3(N, j, k, l), p2 = ijk3(N, j, k, i);
-      sGA[t] = make_uint4(m0 | (m1 << 16), m2 | (m3 << 16), 0u, p0 | (p1 << 10) | (p2 << 20));
-      sGW[t] = make_float4(float(i), float(j), float(k), float(l));
+      // .z: alpha's barycentric indices (i, j, k, l), one byte each
+      sGA[t] = make_uint4(m0 | (m1 << 16), m2 | (m3 << 16),
+                          (uint32_t)i | ((uint32_t)j << 8) | ((uint32_t)k << 16) | ((uint32_t)l << 24),
+                          p0 | (p1 << 10) | (p2 << 20));
       // face nodes: f0 (j=0) at (i,k), f1 (l=0) at (j,k), f2 (i=0) at (j,k), f3 (k=0) at (i,j)
       const uint32_t a0 = j == 0 ? (uint32_t)ij2(N, i, k) : 0xffu;
       const uint32_t a1 = l == 0 ? (uint32_t)ij2(N, j, k) : 0xffu;
@@ -580,11 +580,14 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
         const int n = u + r * TPE;
         if (n >= NP) continue;
         const uint4 ga = sGA[n];
-        const float4 gw4 = sGW[n];
         const int p[4] = {(int)(ga.w & 1023), (int)((ga.w >> 10) & 1023), (int)(ga.w >> 20), n};
         const int xb[4] = {(int)(ga.x & 0xffff), (int)(ga.x >> 16), (int)(ga.y & 0xffff),
                            (int)(ga.y >> 16)};
-        const float ab[4] = {gw4.x, gw4.y, gw4.z, gw4.w};
+        // alpha_b as floats: byte b placed in the mantissa of 2^23, minus 2^23 (exact)
+        float ab[4];
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+          ab[b] = __uint_as_float(__byte_perm(ga.z, 0x4B000000u, 0x7540u + b)) - 8388608.0f;
         // vol(alpha) = sum_b alpha_b w(alpha - e_b), b = 3 first (as the fma nesting before)
         float vol[NW];
         if constexpr (NW == 4) {
