@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "bbdg_internal.cuh"
+#include "bbdg_stack_slots.cuh"
 #include "bbdg_stage_fast.cuh"
 
 namespace {
@@ -67,9 +68,11 @@ struct FastLayout {
   static constexpr int NTE = EPB * TPE;                // element threads
   static constexpr int NT = NTE + CHT;
   // chain stacks: element-face e4 = element * 4 + face holds its NCH chains interleaved,
-  // entry (e4, p, ch) at (e4 * NPS + p) * NCH + ch. NPS = 1 mod 16 puts the same entry of the
-  // 32 chains of a warp (consecutive e4 and ch) in 32 different banks for NCH = 2 and 6.
-  static constexpr int NPS = (NP + 14) / 16 * 16 + 1;
+  // stack entry q of chain ch at ((e4 * NPS + stack_slot<N>(q)) * NCH + ch). NPS = 1 mod 16
+  // puts the same slot of the 32 chains of a warp (consecutive e4 and ch) in 32 different
+  // banks for NCH = 2 and 6; the slots spread the gather's reads over the banks.
+  static constexpr int NSLOT = StackSlots<N>::span > NP ? StackSlots<N>::span : NP;
+  static constexpr int NPS = (NSLOT + 14) / 16 * 16 + 1;
   // w(beta) rows: NPM1 entries, then NZ zero entries from Z0 (a multiple of 8) on, one per bank
   // group of the gather's vector loads (16-byte entries: 8 lanes per phase, 8 groups; 24-byte
   // entries: 16 lanes per phase, bank pair 3 x mod 16); a coefficient with alpha_b = 0 reads the
@@ -99,6 +102,7 @@ struct FastLayout {
   static constexpr int MINB = 2 * BYTES <= 227 * 1024 ? 2 : 1;
   static_assert((EPB * NP * 4) % 16 == 0, "tile segments must be multiples of 16 bytes");
   static_assert(NFP < 255, "face node indices are packed in bytes");
+  static_assert(NPM1P <= 256 && NPS <= 1024, "w indices and stack slots fit the packed table");
   static_assert(TPE % 32 == 0 && TPE >= 32, "element threads come in whole warps");
 };
 
@@ -164,7 +168,8 @@ __device__ __forceinline__ void named_sync(int id, int count) {
 }
 
 // One face lift chain for compile-time N: x = chain input (NFP values, smem); g = the face's
-// volume stack with entries NCH apart, g[c_ijk(N,i,j,d) * NCH] = F_d(i,j) = l_d E_d(i,j). The
+// volume stack with entries NCH apart, g[stack_slot<N>(c_ijk(N,i,j,d)) * NCH] = F_d(i,j) =
+// l_d E_d(i,j) (slots fold to immediates: the loops are unrolled). The
 // chain carries F_d itself: l_d / l_{d-1} = -(N-d+1)/(d+1) and R_{N-d+1} divides by N-d+1, so
 // F_d = -1/(d+1) [(i+1) F_{d-1}(i+1,j) + (j+1) F_{d-1}(i,j+1) + (N-d+1-i-j) F_{d-1}(i,j)]
 // (F_0 = E_0 = L0 x). All of x is read before g is written.
@@ -191,7 +196,7 @@ __device__ __forceinline__ void lift_chain(const float* x, float* g) {
     }
   }
 #pragma unroll
-  for (int m = 0; m < NFP; ++m) g[m * NCH] = E[m];  // layer 0 (c_ijk(N,i,j,0) = c_ij(N,i,j))
+  for (int m = 0; m < NFP; ++m) g[stack_slot<N>(m) * NCH] = E[m];  // layer 0 (c_ijk(N,i,j,0) = c_ij(N,i,j))
 #pragma unroll
   for (int d = 1; d <= N; ++d) {
     const int n = N - d + 1;  // input degree; E indexed with the degree-N layout
@@ -206,7 +211,7 @@ __device__ __forceinline__ void lift_chain(const float* x, float* g) {
                         (float(j + 1) * inv * E[c_ij(N, i, j + 1)] +
                          float(n - i - j) * inv * E[c_ij(N, i, j)]);
         E[c_ij(N, i, j)] = v;
-        g[c_ijk(N, i, j, d) * NCH] = v;
+        g[stack_slot<N>(c_ijk(N, i, j, d)) * NCH] = v;
       }
     }
   }
@@ -320,13 +325,15 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
         while (zs < L::NZ - 1 && ((used >> group_of(L::Z0 + zs)) & 1u)) ++zs;
         mb[b] = (uint32_t)(L::Z0 + zs);
       }
-      const uint32_t m0 = mb[0], m1 = mb[1], m2 = mb[2], m3 = mb[3];
-      // stack positions of this coefficient on faces f0 (i,k,j), f1 (j,k,l), f2 (j,k,i)
-      const uint32_t p0 = ijk3(N, i, k, j), p1 = ijk3(N, j, k, l), p2 = ijk3(N, j, k, i);
-      // .z: alpha's barycentric indices (i, j, k, l), one byte each
-      sGA[t] = make_uint4(m0 | (m1 << 16), m2 | (m3 << 16),
+      // stack slots of this coefficient on faces f0 (i,k,j), f1 (j,k,l), f2 (j,k,i), f3 (i,j,k)
+      const uint32_t p0 = stack_slot<N>(ijk3(N, i, k, j)), p1 = stack_slot<N>(ijk3(N, j, k, l));
+      const uint32_t p2 = stack_slot<N>(ijk3(N, j, k, i)), p3 = stack_slot<N>(t);
+      // .x: w indices of alpha - e_b, one byte each; .z: alpha's barycentric indices
+      // (i, j, k, l), one byte each
+      sGA[t] = make_uint4(mb[0] | (mb[1] << 8) | (mb[2] << 16) | (mb[3] << 24),
+                          p0 | (p1 << 10) | (p2 << 20),
                           (uint32_t)i | ((uint32_t)j << 8) | ((uint32_t)k << 16) | ((uint32_t)l << 24),
-                          p0 | (p1 << 10) | (p2 << 20));
+                          p3);
       // face nodes: f0 (j=0) at (i,k), f1 (l=0) at (j,k), f2 (i=0) at (j,k), f3 (k=0) at (i,j)
       const uint32_t a0 = j == 0 ? (uint32_t)ij2(N, i, k) : 0xffu;
       const uint32_t a1 = l == 0 ? (uint32_t)ij2(N, j, k) : 0xffu;
@@ -580,9 +587,10 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
         const int n = u + r * TPE;
         if (n >= NP) continue;
         const uint4 ga = sGA[n];
-        const int p[4] = {(int)(ga.w & 1023), (int)((ga.w >> 10) & 1023), (int)(ga.w >> 20), n};
-        const int xb[4] = {(int)(ga.x & 0xffff), (int)(ga.x >> 16), (int)(ga.y & 0xffff),
-                           (int)(ga.y >> 16)};
+        const int p[4] = {(int)(ga.y & 1023), (int)((ga.y >> 10) & 1023), (int)(ga.y >> 20),
+                          (int)ga.w};
+        const int xb[4] = {(int)(ga.x & 0xff), (int)((ga.x >> 8) & 0xff), (int)((ga.x >> 16) & 0xff),
+                           (int)(ga.x >> 24)};
         // alpha_b as floats: byte b placed in the mantissa of 2^23, minus 2^23 (exact)
         float ab[4];
 #pragma unroll
