@@ -29,6 +29,17 @@ CANDIDATES = {
     ("wave", 10, torch.float32): [("specialised", 2, 160), ("generic", 4, 256)],
     ("maxwell", 10, torch.float32): [("specialised", 2, 192), ("specialised", 2, 256),
                                      ("generic", 2, 256)],
+    ("wave", 4, torch.float32): [("specialised", 8, 320), ("generic", 8, 256)],
+    ("maxwell", 4, torch.float32): [("specialised", 4, 224), ("generic", 8, 256)],
+    ("wave", 6, torch.float32): [("specialised", 4, 160), ("specialised", 8, 320),
+                                 ("generic", 6, 256)],
+    ("maxwell", 6, torch.float32): [("specialised", 2, 192), ("generic", 6, 256)],
+    ("wave", 7, torch.float32): [("specialised", 4, 288), ("generic", 6, 256)],
+    ("maxwell", 7, torch.float32): [("specialised", 2, 192), ("generic", 6, 256)],
+    ("wave", 8, torch.float32): [("specialised", 4, 288), ("generic", 4, 256)],
+    ("maxwell", 8, torch.float32): [("specialised", 4, 224), ("generic", 4, 256)],
+    ("wave", 11, torch.float32): [("specialised", 2, 224), ("generic", 2, 256)],
+    ("maxwell", 11, torch.float32): [("specialised", 2, 256), ("generic", 2, 256)],
 }
 GENERIC = [("generic", e, 256) for e in (1, 2, 4, 6, 12)]
 

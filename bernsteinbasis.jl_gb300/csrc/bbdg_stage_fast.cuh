@@ -19,7 +19,8 @@ struct FastStageParams {
   int* status;
   // volume phase: warp-round g = r * (TPE / 32) + warp forms w(beta) for beta = vstart[g] +
   // lane, lane < vlen[g] (filled by the launcher)
-  uint8_t vstart[16], vlen[16];
+  uint16_t vstart[16];
+  uint8_t vlen[16];
 };
 
 struct FastLaunch {

@@ -144,3 +144,28 @@ def test_meshdata_import_rejects_a_broken_mapP(bb):
     nJ = md.nJ.reshape(m.K, 4, bb.np2(2), 3)[:, :, 0, :]
     with pytest.raises(ValueError):
         from_meshdata(2, md.Fmask, bad, md.geo9, nJ, md.Jall)
+
+
+def test_stack_slot_header_is_generated_and_injective():
+    """The committed lift-stack slot table is what its generator produces, and every degree's
+    slots are distinct and fit the stack stride the stage kernel reserves."""
+    import re
+    import subprocess
+    import sys
+    csrc = os.path.join(os.path.dirname(__file__), "..", "bernsteinbasis.jl_gb300", "csrc")
+    with open(os.path.join(csrc, "bbdg_stack_slots.cuh")) as fh:
+        committed = fh.read()
+    produced = subprocess.run([sys.executable, os.path.join(csrc, "gen_stack_slots.py")],
+                              capture_output=True, text=True, check=True).stdout
+    assert produced == committed
+    for block in re.findall(r"stack_slot<(\d+)>\(int q\) \{(.*?)\n\}", committed, re.S):
+        N = int(block[0])
+        NP = (N + 1) * (N + 2) * (N + 3) // 6
+        table = dict((int(a), int(b)) for a, b in re.findall(r"case (\d+): return (\d+);", block[1]))
+        slots = [table.get(q, q) for q in range(NP)]
+        assert len(set(slots)) == NP
+        span = int(re.search(rf"struct StackSlots<{N}> \{{\s*static constexpr int span = (\d+);",
+                             committed).group(1))
+        assert max(slots) + 1 == span
+        nps = (max(NP, span) + 14) // 16 * 16 + 1
+        assert span <= nps and nps % 16 == 1
