@@ -23,18 +23,19 @@ CANDIDATES = {
     ("maxwell", 9, torch.float32): [("specialised", 2, 192), ("specialised", 2, 256),
                                     ("generic", 2, 256)],
     ("wave", 5, torch.float32): [("specialised", 4, 160), ("specialised", 8, 320),
-                                 ("generic", 8, 256)],
+                                 ("specialised", 2, 96), ("generic", 8, 256)],
     ("maxwell", 5, torch.float32): [("specialised", 4, 224), ("specialised", 8, 448),
-                                    ("generic", 8, 256)],
+                                    ("specialised", 2, 128), ("generic", 8, 256)],
     ("wave", 10, torch.float32): [("specialised", 2, 160), ("generic", 4, 256)],
     ("maxwell", 10, torch.float32): [("specialised", 2, 192), ("specialised", 2, 256),
                                      ("generic", 2, 256)],
     ("wave", 4, torch.float32): [("specialised", 8, 320), ("generic", 8, 256)],
     ("maxwell", 4, torch.float32): [("specialised", 4, 224), ("generic", 8, 256)],
     ("wave", 6, torch.float32): [("specialised", 4, 160), ("specialised", 8, 320),
-                                 ("generic", 6, 256)],
+                                 ("specialised", 2, 160), ("generic", 6, 256)],
     ("maxwell", 6, torch.float32): [("specialised", 2, 192), ("generic", 6, 256)],
-    ("wave", 7, torch.float32): [("specialised", 4, 288), ("generic", 6, 256)],
+    ("wave", 7, torch.float32): [("specialised", 4, 288), ("specialised", 2, 160),
+                                 ("generic", 6, 256)],
     ("maxwell", 7, torch.float32): [("specialised", 2, 192), ("generic", 6, 256)],
     ("wave", 8, torch.float32): [("specialised", 4, 288), ("generic", 4, 256)],
     ("maxwell", 8, torch.float32): [("specialised", 4, 224), ("generic", 4, 256)],

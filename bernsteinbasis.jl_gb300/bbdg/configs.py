@@ -158,13 +158,19 @@ def config4(steps: int = 100, dtype=torch.float32, compare_single: bool = True):
            "tiles_per_N": tiles,
            "problems_list": [[s.physics, s.N, s.n, m.K] for s, m in zip(specs, B.meshes)]}
     if compare_single:
-        # the same problems advanced one solver at a time (5 launches per problem per step)
+        # the same problems advanced one solver at a time (5 launches per problem per step),
+        # each with the kernel the batch runs it on: the degree-specialised kernel where one
+        # exists for (N, physics, K), else the generic kernel with the batch's tile
         solvers = []
+        fast = 0
         for p, s in enumerate(specs):
             sv = DGSolver(B.meshes[p], s.N, s.physics, dtype=dtype, tau=s.tau)
-            sv.set_kernel("generic")
-            sv.set_tile(B.tile(s.physics, s.N), 256)
+            if sv.kernel == "generic":
+                sv.set_tile(B.tile(s.physics, s.N), 256)
+            else:
+                fast += 1
             solvers.append((sv, B.q[p].clone(), torch.zeros_like(B.q[p]), B.dt(p)))
+        res["fast_lanes"] = fast
         for sv, q, r, dt in solvers:
             sv.run(q, r, dt, 1)
         torch.cuda.synchronize()

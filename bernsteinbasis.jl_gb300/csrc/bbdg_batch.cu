@@ -1,23 +1,29 @@
 // Batched persistent stage kernel: many independent wave / Maxwell problems of uneven
-// degree N and element count K advance together, one launch per LSRK stage.
+// degree N and element count K advance together.
 //
-// Work items are (problem, element tile) pairs, numbered problem by problem; the blocks of a
-// persistent grid draw items from a device counter (one 64-bit atomicAdd per item, no
-// spinning) and run the generic stage tile (bbdg_stage_generic.cuh) for that problem,
-// reloading the degree tables into shared memory only when the problem changes. Each problem
-// keeps its own time step, tile shape (chosen per degree), trace buffers and state; a step
-// (5 stages + the counter reset) is replayed from a CUDA graph.
+// FP32 problems with a degree-specialised stage kernel for their (N, physics) and element
+// count ("fast lanes") run that kernel, each problem its own persistent launch per stage on
+// one of several side streams, so that small problems share the GPU. The other problems run
+// the batched generic kernel: work items are (problem, element tile) pairs, numbered problem
+// by problem; the blocks of a persistent grid draw items from a device counter (one 64-bit
+// atomicAdd per item, no spinning) and run the generic stage tile (bbdg_stage_generic.cuh)
+// for that problem, reloading the degree tables into shared memory only when the problem
+// changes. Each problem keeps its own time step, tile shape, trace buffers and state; a step
+// (5 stages of every lane + the counter reset, forked and joined by events) is replayed from
+// a CUDA graph.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
 #include "bbdg_internal.cuh"
+#include "bbdg_stage_fast.cuh"
 #include "bbdg_stage_generic.cuh"
 
 namespace {
 
 constexpr int kBatchThreads = 256;
+constexpr int kSideStreams = 8;  // streams the fast lanes are spread over
 const double kA[5] = {0.0, -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
                       -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0};
 const double kB[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13612068292357.0,
@@ -113,6 +119,8 @@ struct bb_batch {
   std::vector<bb_batch_problem> probs;
   std::vector<const DegTables*> tabs;
   std::vector<int> epb;          // per problem
+  std::vector<int> fast;         // per problem: specialised variant, -1 = generic kernel
+  int nfast = 0, ngeneric = 0;
   std::vector<void*> trace;      // 2 per problem
   void* d_desc = nullptr;
   unsigned long long* d_counter = nullptr;  // 5 stage counters
@@ -122,6 +130,8 @@ struct bb_batch {
   int grid = 0;
   bool dirty = true;             // descriptors need rebuilding
   cudaStream_t cap = nullptr;
+  cudaStream_t side[kSideStreams] = {};
+  cudaEvent_t fork_ev = nullptr, join_ev[kSideStreams] = {};
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
 };
 
@@ -149,13 +159,29 @@ template <class T>
 int build_desc(bb_batch* b) {
   bb_ctx* ctx = b->ctx;
   const int np = (int)b->probs.size();
-  std::vector<BatchDesc<T>> h(np);
+  auto a16 = [](const void* x) { return ((uintptr_t)x & 15) == 0; };
+  b->fast.assign(np, -1);
+  b->nfast = b->ngeneric = 0;
+  for (int p = 0; p < np; ++p) {
+    const bb_batch_problem& pr = b->probs[p];
+    if (sizeof(T) == 4 && a16(pr.q) && a16(pr.res) && a16(pr.geo) && a16(pr.conn)) {
+      const int idx = bb_fast_find(pr.N, pr.physics, 0, 0, pr.K);
+      int e = 0, th = 0;
+      size_t sm = 0;
+      if (idx >= 0 && bb_fast_variant_info(idx, &e, &th, &sm) == BB_OK && sm <= ctx->smem_optin)
+        b->fast[p] = idx;
+    }
+    if (b->fast[p] >= 0) ++b->nfast;
+  }
+  std::vector<BatchDesc<T>> h;
   int64_t begin = 0;
   size_t smem = 0;
   for (int p = 0; p < np; ++p) {
+    if (b->fast[p] >= 0) continue;
     const bb_batch_problem& pr = b->probs[p];
     const DegTables* t = b->tabs[p];
-    BatchDesc<T>& d = h[p];
+    h.emplace_back();
+    BatchDesc<T>& d = h.back();
     memset(&d, 0, sizeof(d));
     d.P.tab = *t;
     d.P.gtab = t->d_words;
@@ -180,13 +206,18 @@ int build_desc(bb_batch* b) {
                                          kBatchChainLiftBytes);
     smem = std::max(smem, L.total);
   }
+  b->ngeneric = (int)h.size();
+  b->total = begin;
+  b->smem = smem;
+  if (h.empty()) {
+    b->dirty = false;
+    return BB_OK;
+  }
   if (smem > ctx->smem_optin) return bb_fail(ctx, BB_ERR_ARG, "batch tiles exceed shared memory");
   if (!b->d_desc) {
     BB_CUDA(ctx, cudaMalloc(&b->d_desc, sizeof(BatchDesc<T>) * np));
   }
-  BB_CUDA(ctx, cudaMemcpy(b->d_desc, h.data(), sizeof(BatchDesc<T>) * np, cudaMemcpyHostToDevice));
-  b->total = begin;
-  b->smem = smem;
+  BB_CUDA(ctx, cudaMemcpy(b->d_desc, h.data(), sizeof(BatchDesc<T>) * h.size(), cudaMemcpyHostToDevice));
   BB_CUDA(ctx, cudaFuncSetAttribute(batch_stage_kernel<T>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
@@ -198,15 +229,69 @@ int build_desc(bb_batch* b) {
   return BB_OK;
 }
 
+// Stage s of a fast-lane problem: its specialised kernel, traces in buffer (par + s) & 1.
+int launch_fast_lane(bb_batch* b, int p, int s, int par, cudaStream_t st) {
+  const bb_batch_problem& pr = b->probs[p];
+  const DegTables& t = *b->tabs[p];
+  FastStageParams P{};
+  P.gtab = t.d_words;
+  P.o_node3 = t.o_node3;
+  P.o_node3m1 = t.o_node3m1;
+  P.o_fvol = t.o_fvol;
+  P.o_fperm = t.o_fperm;
+  P.K = pr.K;
+  P.mode = 1;
+  P.rkA = float(kA[s]);
+  P.rkB = float(kB[s]);
+  P.dt = float(pr.dt);
+  P.tau = float(pr.tau);
+  P.q = (float*)pr.q;
+  P.res = (float*)pr.res;
+  P.rhs = nullptr;
+  const int in = (par + s) & 1;
+  P.trace_in = (const float*)b->trace[2 * p + in];
+  P.trace_out = (float*)b->trace[2 * p + (in ^ 1)];
+  P.geo = (const float*)pr.geo;
+  P.conn = pr.conn;
+  P.status = b->d_status;
+  FastLaunch fl;
+  fl.num_sms = b->ctx->num_sms;
+  const int rc = bb_fast_launch(b->fast[p], fl, P, st);
+  if (rc) return bb_fail(b->ctx, rc, "stage_fast_kernel launch: %s", cudaGetErrorString(cudaGetLastError()));
+  b->ctx->launches++;
+  return BB_OK;
+}
+
 template <class T>
 int enqueue_batch_step(bb_batch* b, int par, cudaStream_t st) {
-  BB_CUDA(b->ctx, cudaMemsetAsync(b->d_counter, 0, 5 * sizeof(unsigned long long), st));
-  for (int s = 0; s < 5; ++s) {
-    batch_stage_kernel<T><<<b->grid, kBatchThreads, b->smem, st>>>(
-        (const BatchDesc<T>*)b->d_desc, (int)b->probs.size(), b->total, b->d_counter + s,
-        (par + s) & 1, T(kA[s]), T(kB[s]));
-    int rc = bb_check_launch(b->ctx, "batch_stage_kernel");
-    if (rc) return rc;
+  bb_ctx* ctx = b->ctx;
+  const int nside = std::min(b->nfast, kSideStreams);
+  if (nside > 0) {  // fork: the fast lanes start with the step
+    BB_CUDA(ctx, cudaEventRecord(b->fork_ev, st));
+    for (int i = 0; i < nside; ++i) BB_CUDA(ctx, cudaStreamWaitEvent(b->side[i], b->fork_ev, 0));
+    int j = 0;
+    for (size_t p = 0; p < b->probs.size(); ++p) {
+      if (b->fast[p] < 0) continue;
+      cudaStream_t ss = b->side[j++ % nside];
+      for (int s = 0; s < 5; ++s) {
+        const int rc = launch_fast_lane(b, (int)p, s, par, ss);
+        if (rc) return rc;
+      }
+    }
+  }
+  if (b->ngeneric > 0) {
+    BB_CUDA(ctx, cudaMemsetAsync(b->d_counter, 0, 5 * sizeof(unsigned long long), st));
+    for (int s = 0; s < 5; ++s) {
+      batch_stage_kernel<T><<<b->grid, kBatchThreads, b->smem, st>>>(
+          (const BatchDesc<T>*)b->d_desc, b->ngeneric, b->total, b->d_counter + s,
+          (par + s) & 1, T(kA[s]), T(kB[s]));
+      int rc = bb_check_launch(ctx, "batch_stage_kernel");
+      if (rc) return rc;
+    }
+  }
+  for (int i = 0; i < nside; ++i) {  // join
+    BB_CUDA(ctx, cudaEventRecord(b->join_ev[i], b->side[i]));
+    BB_CUDA(ctx, cudaStreamWaitEvent(st, b->join_ev[i], 0));
   }
   return BB_OK;
 }
@@ -280,6 +365,11 @@ void free_batch(bb_batch* b) {
   cudaFree(b->d_counter);
   cudaFree(b->d_status);
   if (b->cap) cudaStreamDestroy(b->cap);
+  for (int i = 0; i < kSideStreams; ++i) {
+    if (b->side[i]) cudaStreamDestroy(b->side[i]);
+    if (b->join_ev[i]) cudaEventDestroy(b->join_ev[i]);
+  }
+  if (b->fork_ev) cudaEventDestroy(b->fork_ev);
   delete b;
 }
 
@@ -327,10 +417,17 @@ extern "C" int bb_batch_create(bb_ctx* ctx, int nprob, const bb_batch_problem* p
   if (cudaMalloc(&b->d_counter, 5 * sizeof(unsigned long long)) != cudaSuccess ||
       cudaMalloc(&b->d_status, sizeof(int)) != cudaSuccess ||
       cudaMemset(b->d_status, 0, sizeof(int)) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming) != cudaSuccess) {
     free_batch(b);
     return bb_fail(ctx, BB_ERR_NOMEM, "batch allocation failed");
   }
+  for (int i = 0; i < kSideStreams; ++i)
+    if (cudaStreamCreateWithFlags(&b->side[i], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->join_ev[i], cudaEventDisableTiming) != cudaSuccess) {
+      free_batch(b);
+      return bb_fail(ctx, BB_ERR_NOMEM, "batch stream allocation failed");
+    }
   *out = b;
   return BB_OK;
 }

@@ -11,3 +11,6 @@ template int bbfast::launch_fast_t<4, BB_MAXWELL, 4, 32>(const FastLaunch&, cons
 template int bbfast::launch_fast_t<6, BB_WAVE, 4, 32>(const FastLaunch&, const FastStageParams&, cudaStream_t);
 template int bbfast::launch_fast_t<6, BB_WAVE, 8, 32>(const FastLaunch&, const FastStageParams&, cudaStream_t);
 template int bbfast::launch_fast_t<6, BB_MAXWELL, 2, 64>(const FastLaunch&, const FastStageParams&, cudaStream_t);
+template int bbfast::launch_fast_t<5, BB_WAVE, 2, 32>(const FastLaunch&, const FastStageParams&, cudaStream_t);
+template int bbfast::launch_fast_t<6, BB_WAVE, 2, 64>(const FastLaunch&, const FastStageParams&, cudaStream_t);
+template int bbfast::launch_fast_t<5, BB_MAXWELL, 2, 32>(const FastLaunch&, const FastStageParams&, cudaStream_t);

@@ -6,3 +6,4 @@ template int bbfast::launch_fast_t<7, BB_WAVE, 4, 64>(const FastLaunch&, const F
 template int bbfast::launch_fast_t<7, BB_MAXWELL, 2, 64>(const FastLaunch&, const FastStageParams&, cudaStream_t);
 template int bbfast::launch_fast_t<8, BB_WAVE, 4, 64>(const FastLaunch&, const FastStageParams&, cudaStream_t);
 template int bbfast::launch_fast_t<8, BB_MAXWELL, 4, 32>(const FastLaunch&, const FastStageParams&, cudaStream_t);
+template int bbfast::launch_fast_t<7, BB_WAVE, 2, 64>(const FastLaunch&, const FastStageParams&, cudaStream_t);

@@ -160,9 +160,11 @@ int bb_project(bb_ctx* ctx, int N, int M, int64_t K, int nf, int dtype_in, const
 
 /* ---- batched uneven solves ------------------------------------------------------------
  * Many independent wave / Maxwell problems of different degree N and element count K advance
- * together: one persistent launch per LSRK stage whose blocks draw (problem, element tile)
- * work items from a device counter, each step replayed from a CUDA graph. Each problem keeps
- * its own time step and penalty; the tile shape is chosen per (physics, N). No counterpart in
+ * together, each step replayed from a CUDA graph. FP32 problems with a degree-specialised
+ * stage kernel for their (N, physics, K) run it on side streams (one persistent launch per
+ * problem and stage); the others share one persistent launch per stage whose blocks draw
+ * (problem, element tile) work items from a device counter. Each problem keeps its own time
+ * step and penalty; the generic tile shape is chosen per (physics, N). No counterpart in
  * the reference, which solves one problem per script (examples/3d_wave.jl,
  * examples/3d_maxwell.jl). Arrays are device pointers in the batch dtype and must outlive
  * the batch object. */

@@ -53,3 +53,29 @@ def test_batch_graph_equals_stream_fp32(cuda, bb):
     torch.cuda.synchronize()
     for qa, qb in zip(A.q, B.q):
         assert torch.equal(qa, qb)
+
+
+def test_batch_fast_lanes_match_single_solves(cuda, bb):
+    """FP32: problems with a degree-specialised kernel for their (N, physics, K) run it as
+    fast lanes on side streams, the others the batched generic kernel; every problem ends
+    bitwise equal to a single solver making the same kernel choice (graph replay)."""
+    import torch
+    from bbdg.batch import BatchSolver, ProblemSpec
+    sp = specs() + [ProblemSpec("maxwell", 9, 2, seed=7), ProblemSpec("wave", 6, 3, seed=8),
+                    ProblemSpec("wave", 7, 2, seed=9)]
+    B = BatchSolver(sp, dtype=torch.float32)
+    q0 = [q.clone() for q in B.q]
+    B.run(3, graph=True)
+    torch.cuda.synchronize()
+    kinds = set()
+    for p, spec in enumerate(B.specs):
+        s = bb.DGSolver(B.meshes[p], spec.N, spec.physics, dtype=torch.float32, tau=spec.tau)
+        if s.kernel == "generic":
+            s.set_tile(B.tile(spec.physics, spec.N), 256)
+        kinds.add(s.kernel)
+        q = q0[p].clone()
+        r = torch.zeros_like(q)
+        s.run(q, r, B.dt(p), 3, graph=True)
+        torch.cuda.synchronize()
+        assert torch.equal(q, B.q[p]), (p, s.kernel)
+    assert kinds == {"generic", "specialised"}

@@ -163,15 +163,15 @@ def test_corrupt_connectivity_is_reported(cuda, bb):
 
 FAST_TILES = {("wave", 9): [(4, 288), (4, 160), (2, 160)],
               ("maxwell", 9): [(2, 192), (2, 256)],
-              ("wave", 5): [(4, 160), (8, 320)],
-              ("maxwell", 5): [(4, 224), (8, 448)],
+              ("wave", 5): [(4, 160), (8, 320), (2, 96)],
+              ("maxwell", 5): [(4, 224), (8, 448), (2, 128)],
               ("wave", 10): [(2, 160)],
               ("maxwell", 10): [(2, 192), (2, 256)],
               ("wave", 4): [(8, 320)],
               ("maxwell", 4): [(4, 224)],
-              ("wave", 6): [(4, 160), (8, 320)],
+              ("wave", 6): [(4, 160), (8, 320), (2, 160)],
               ("maxwell", 6): [(2, 192)],
-              ("wave", 7): [(4, 288)],
+              ("wave", 7): [(4, 288), (2, 160)],
               ("maxwell", 7): [(2, 192)],
               ("wave", 8): [(4, 288)],
               ("maxwell", 8): [(4, 224)],
