@@ -456,6 +456,10 @@ static int grid_for(bb_ctx* ctx, int64_t nblk, int per_sm) {
 template <class T>
 static int launch_deriv(bb_ctx* ctx, const DegTables* t, int64_t K, int mask, const void* x,
                         void* o0, void* o1, void* o2, cudaStream_t st) {
+  if (sizeof(T) == 4) {
+    const int rc = bb_deriv_fast(ctx, t, K, mask, x, o0, o1, o2, st);
+    if (rc >= 0) return rc;  // otherwise no specialised kernel for this degree or mask
+  }
   {
     // factored kernel: tile of epb elements plus the w rows and the index tables
     int epb = 16;

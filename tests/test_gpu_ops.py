@@ -67,6 +67,40 @@ def test_lift_matches_oracle(cuda, bb, oracle_cpu, N, dt, K):
     assert rel(of.cpu().numpy(), want) < TOL[dt]
 
 
+@pytest.mark.parametrize("N", [1, 4, 8, 9, 10, 12])
+def test_deriv_fp32_many_tiles_and_misaligned(cuda, bb, oracle_cpu, N):
+    """K = 20011 gives more tiles than the one-warp blocks of the degree-specialised FP32
+    derivative kernel, and a ragged last tile whose inputs end inside a float4 for odd Np; a
+    sample of columns is checked against the oracle for each axis, the fused gradient equals
+    the single-axis results bitwise, and misaligned columns (the generic kernel) agree."""
+    import torch
+    rng = np.random.default_rng(110 + N)
+    K = 20011
+    Np = bb.np3(N)
+    x = rng.uniform(-1, 1, (K, Np)).astype(np.float32)
+    xd = torch.tensor(x, device=cuda)
+    cols = np.r_[0:30, K // 2:K // 2 + 30, K - 30:K]
+    outs = []
+    for axis, D in enumerate((bb.BernsteinDerivativeMatrix_3D_r, bb.BernsteinDerivativeMatrix_3D_s,
+                              bb.BernsteinDerivativeMatrix_3D_t)):
+        o = torch.empty_like(xd)
+        bb.mul_(o, D(N), xd)
+        outs.append(o)
+        want = oracle_cpu.deriv(axis, N, x[cols].astype(np.float64))
+        assert rel(o.cpu().numpy()[cols], want) < TOL["f32"], axis
+    g = [torch.empty_like(xd) for _ in range(3)]
+    bb.grad_(g[0], g[1], g[2], N, xd)
+    for a in range(3):
+        assert torch.equal(g[a], outs[a])
+    Km = 257
+    xb = torch.tensor(np.concatenate([[0.0], x[:Km].ravel()]).astype(np.float32), device=cuda)
+    xm = xb[1:].view(Km, Np)
+    assert xm.data_ptr() % 16 != 0
+    om = torch.empty((Km, Np), dtype=torch.float32, device=cuda)
+    bb.mul_(om, bb.BernsteinDerivativeMatrix_3D_s(N), xm)
+    assert rel(om.cpu().numpy(), outs[1][:Km].cpu().numpy()) < TOL["f32"]
+
+
 @pytest.mark.parametrize("N", [3, 9, 10, 12])
 def test_lift_fp32_many_tiles_and_misaligned(cuda, bb, oracle_cpu, N):
     """K = 20011 gives more 8-element tiles than the grid has blocks, so every block works
