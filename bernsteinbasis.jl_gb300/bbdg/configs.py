@@ -255,10 +255,13 @@ def main():
                     help="device memory for the training snapshot store (per phase)")
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--degrees", type=str, default="3-15")
+    ap.add_argument("--state-gb", type=float, default=2.0,
+                    help="config 2: bytes of operator input state per operator, in GB")
+    ap.add_argument("--dtypes", type=str, default="f32,f64", help="config 2: f32, f64 or both")
     a = ap.parse_args()
     if a.config == 2:
         lo, hi = (int(v) for v in a.degrees.split("-"))
-        config2(range(lo, hi + 1))
+        config2(range(lo, hi + 1), dtypes=tuple(a.dtypes.split(",")), state_bytes=a.state_gb * 1e9)
     elif a.config == 3:
         config3(steps=a.steps or 200)
     elif a.config == 4:
