@@ -638,7 +638,13 @@ extern "C" int bb_fused_apply(bb_ctx* ctx, int N, int64_t K, int dtype, const vo
   if (!x || !faces || !dr || !ds || !dt || !lift) return bb_fail(ctx, BB_ERR_ARG, "null pointer");
   const DegTables* t = bb_tables(ctx, N);
   if (!t) return bb_fail(ctx, BB_ERR_NOMEM, "table allocation failed");
-  return dtype == BB_F64
-             ? launch_fused<double>(ctx, t, K, x, faces, dr, ds, dt, lift, (cudaStream_t)stream)
-             : launch_fused<float>(ctx, t, K, x, faces, dr, ds, dt, lift, (cudaStream_t)stream);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (dtype == BB_F32 && N <= 12) {
+    // the gradient and lift calls back to back (degree-specialised kernels where they exist)
+    // move the same bytes faster than the one-launch table-driven pass
+    rc = launch_deriv<float>(ctx, t, K, 7, x, dr, ds, dt, st);
+    return rc ? rc : launch_lift<float>(ctx, t, K, 4, faces, lift, st);
+  }
+  return dtype == BB_F64 ? launch_fused<double>(ctx, t, K, x, faces, dr, ds, dt, lift, st)
+                         : launch_fused<float>(ctx, t, K, x, faces, dr, ds, dt, lift, st);
 }

@@ -163,6 +163,29 @@ def test_fused_operator_pass(cuda, bb, N):
     assert torch.equal(li, ref[3])
 
 
+@pytest.mark.parametrize("N", [3, 9, 12])
+def test_fused_operator_pass_fp32(cuda, bb, oracle_cpu, N):
+    """FP32 (N <= 12): the fused pass is the gradient and lift calls back to back and equals
+    them bitwise; it matches the oracle at 1e-5."""
+    import torch
+    rng = np.random.default_rng(95 + N)
+    K = 301
+    xh = rng.uniform(-1, 1, (K, bb.np3(N)))
+    fh = rng.uniform(-1, 1, (K, 4 * bb.np2(N)))
+    x = torch.tensor(xh, dtype=torch.float32, device=cuda)
+    f = torch.tensor(fh, dtype=torch.float32, device=cuda)
+    dr, ds, dt_, li = (torch.empty_like(x) for _ in range(4))
+    bb.fused_apply_(dr, ds, dt_, li, N, x, f)
+    ref = [torch.empty_like(x) for _ in range(4)]
+    bb.grad_(ref[0], ref[1], ref[2], N, x)
+    bb.mul_(ref[3], bb.BernsteinLift(N), f)
+    for a, b in zip((dr, ds, dt_, li), ref):
+        assert torch.equal(a, b)
+    for axis, a in enumerate((dr, ds, dt_)):
+        assert rel(a.cpu().numpy(), oracle_cpu.deriv(axis, N, xh)) < TOL["f32"]
+    assert rel(li.cpu().numpy(), oracle_cpu.lift(N, fh)) < TOL["f32"]
+
+
 def _golden():
     path = os.path.join(os.path.dirname(__file__), "golden", "operators_exact.json")
     with open(path) as fh:
