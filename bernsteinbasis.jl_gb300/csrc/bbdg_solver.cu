@@ -291,14 +291,16 @@ extern "C" int bb_solver_create(bb_ctx* ctx, int physics, int N, int64_t K, int 
   s->geo = geo;
   s->tau = tau;
   s->tab = t;
-  // default tile: the largest of 12, 6, 4, 2, 1 elements whose tile runs the chain lift
-  // (fits in its shared-memory budget), else the largest that fits in 100 KB
-  const int cands[5] = {12, 6, 4, 2, 1};
+  // default tile: the largest of 12, 6, 4, 2 elements whose tile runs the chain lift (fits
+  // in its shared-memory budget); else, in this order, 4, 2, 6, 12 or 1 elements within
+  // 100 KB (a one-element chain tile ran 1.5x slower than four-element level-parallel
+  // tiles in FP64 at N = 9)
+  const int cands[2][5] = {{12, 6, 4, 2, 0}, {4, 2, 6, 12, 1}};
   for (int pass = 0; pass < 2 && !s->epb; ++pass)
-    for (int c : cands) {
+    for (int c : cands[pass]) {
       size_t sm = 0;
       int chain = 0;
-      if (solver_layout(s, c, &sm, &chain) == BB_OK && sm <= 100 * 1024 &&
+      if (c > 0 && solver_layout(s, c, &sm, &chain) == BB_OK && sm <= 100 * 1024 &&
           (pass == 1 || chain)) {
         s->epb = c;
         s->smem = sm;
