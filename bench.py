@@ -168,6 +168,20 @@ def reference_arm(args, rank):
     return 0
 
 
+def replica_rate(ms_local: float, units_per_rank: float, dist=None, device=None):
+    """Whole-job rate of N independent replicas: every rank processed `units_per_rank` units
+    in its own `ms_local` milliseconds; the job took the slowest rank's time (all-reduce MAX
+    over the process group, when there is one), so the rate is world * units / max time.
+    Returns (max milliseconds, units per second)."""
+    import torch
+    world = dist.get_world_size() if dist else 1
+    t = torch.tensor([ms_local], dtype=torch.float64, device=device)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    return ms_max, world * units_per_rank / (ms_max * 1e-3)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -244,14 +258,10 @@ def main():
     clocks = sampler.stop()
     launches = solver.ctx.launch_count() - launches0
     ms = e0.elapsed_time(e1)
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
     K = mesh.K
     Np = solver.Np
     dof = NF * Np * K
-    value = world * dof * args.steps / (ms_max * 1e-3)
+    ms_max, value = replica_rate(ms, dof * args.steps, dist, device="cuda")
     stage_ms = ms / (5 * args.steps)
     bpe = stage_bytes_per_element()
     peak, peak_kind = peaks()
@@ -271,10 +281,7 @@ def main():
     c1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = c0.elapsed_time(c1) / args.e2e_steps
-    te = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_value = world * dof / (float(te.item()) * 1e-3)
+    _, e2e_value = replica_rate(e2e_ms, dof, dist, device="cuda")
     state_bytes = q.numel() * q.element_size()
 
     # traffic per launch from the committed ncu summary (scaled from the captured case)
