@@ -151,23 +151,6 @@ __device__ __forceinline__ void tma_load(void* dst, const void* src, uint32_t by
 __device__ __forceinline__ void l2_prefetch(const void* src, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
 }
-__device__ __forceinline__ void tma_store(void* dst, const void* src, uint32_t bytes) {
-  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst),
-               "r"(s_addr(src)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void tma_store_commit() {
-  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-}
-__device__ __forceinline__ void tma_store_wait_read() {
-  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-}
-__device__ __forceinline__ void tma_store_wait_all() {
-  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
-}
-__device__ __forceinline__ void named_sync(int id, int count) {
-  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
 
 // One face lift chain for compile-time N: x = chain input (NFP values, smem); g = the face's
 // volume stack with entries NCH apart, g[stack_slot<N>(c_ijk(N,i,j,d)) * NCH] = F_d(i,j) =
@@ -724,7 +707,6 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
     // let copies still in flight land before the block exits (bounded)
     for (int b = 0; b < 3; ++b) mbar_wait(&bar[b], (ph >> b) & 1u);
   }
-  if (tid == 0) tma_store_wait_all();
 }
 
 // Volume-phase work split (host, once per variant): the NPM1 points beta, in index order, are
