@@ -3,7 +3,8 @@
 For a solver it times every compiled tile variant (elements per block x threads per
 block; degree-specialised FP32 variants and the generic kernel) over a few LSRK steps on the
 solver's own mesh with CUDA events, keeps the fastest, and caches the choice per
-(physics, N, dtype, device name) in a JSON file next to the built library.
+(physics, N, dtype, element count, device name) in a JSON file next to the built library
+(the element count decides which tiles divide the mesh).
 """
 from __future__ import annotations
 
@@ -47,7 +48,7 @@ GENERIC = [("generic", e, 256) for e in (1, 2, 4, 6, 12)]
 
 def _key(solver) -> str:
     name = torch.cuda.get_device_name(solver.device)
-    return f"{solver.physics}|{solver.N}|{str(solver.dtype)}|{name}"
+    return f"{solver.physics}|{solver.N}|{str(solver.dtype)}|K={solver.K}|{name}"
 
 
 def _load():
@@ -68,9 +69,13 @@ def tune(solver, steps: int = 3, use_cache: bool = True, verbose: bool = False):
     cache = _load() if use_cache else {}
     if key in cache:
         kind, epb, nt = cache[key]["choice"]
-        solver.set_kernel(kind)
-        solver.set_tile(epb, nt)
-        return (kind, epb, nt), cache[key]["ms_per_step"]
+        try:
+            solver.set_kernel(kind)
+            solver.set_tile(epb, nt)
+            if solver.kernel == kind:
+                return (kind, epb, nt), cache[key]["ms_per_step"]
+        except Exception:  # a stale entry: tune again
+            pass
     q = (torch.rand((solver.nf, solver.K, solver.Np), dtype=solver.dtype,
                     device=solver.device) - 0.5) * 1e-3
     r = torch.zeros_like(q)
