@@ -239,6 +239,7 @@ int launch_fast_lane(bb_batch* b, int p, int s, int par, cudaStream_t st) {
   P.o_node3m1 = t.o_node3m1;
   P.o_fvol = t.o_fvol;
   P.o_fperm = t.o_fperm;
+  P.o_sslot = t.o_sslot;
   P.K = pr.K;
   P.mode = 1;
   P.rkA = float(kA[s]);

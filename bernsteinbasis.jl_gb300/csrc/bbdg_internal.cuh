@@ -71,6 +71,7 @@ struct DegTables {
   int o_fvol = 0;    // 4*Nfp uint16: face node -> volume index
   int o_fperm = 0;   // 6*Nfp uint16: face node -> neighbour face node, per orientation
   int o_fstack = 0;  // 4*Np uint16: face f's lift stack entry (layer, node) -> volume index
+  int o_sslot = 0;   // Np uint16: stage-kernel stack slot of lift-stack entry q (stack_slot<N>)
   int nwords = 0;
   uint32_t* d_words = nullptr;
   double* d_lj = nullptr;  // N+1 entries, d_lj[j] = l_j(N) (constants.jl:10-12), [0] = 0

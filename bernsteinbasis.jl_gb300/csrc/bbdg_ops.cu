@@ -8,6 +8,7 @@
 #include <cstring>
 
 #include "bbdg_internal.cuh"
+#include "bbdg_stack_slots.cuh"
 
 // -------------------------------------------------------------------------------------
 // context
@@ -86,6 +87,15 @@ extern "C" const char* bb_ctx_last_error(const bb_ctx* ctx) {
 extern "C" int64_t bb_ctx_launch_count(const bb_ctx* ctx) { return ctx ? ctx->launches : -1; }
 
 // l_j(N) = (-1)^j C(N, j) / (1 + j)  (src/constants.jl:10-12)
+// Stage-kernel lift-stack slot of entry q (the generated tables of bbdg_stack_slots.cuh).
+static int stack_slot_of(int N, int q) {
+  switch (N) {
+    case 9: return stack_slot<9>(q);
+    case 10: return stack_slot<10>(q);
+    default: return q;
+  }
+}
+
 static double lift_lj(int N, int j) {
   double b = 1.0;
   for (int m = 1; m <= j; ++m) b = b * (N - j + m) / m;
@@ -109,6 +119,7 @@ const DegTables* bb_tables(bb_ctx* ctx, int N) {
   t->o_fvol = off; off += (4 * t->Nfp + 1) / 2;
   t->o_fperm = off; off += (6 * t->Nfp + 1) / 2;
   t->o_fstack = off; off += (4 * t->Np + 1) / 2;
+  t->o_sslot = off; off += (t->Np + 1) / 2;
   t->nwords = off;
   std::vector<uint32_t> w(off, 0u);
   auto put16 = [&](int word_off, int idx, int v) {
@@ -151,6 +162,7 @@ const DegTables* bb_tables(bb_ctx* ctx, int N) {
       for (int b = 0; b <= N - d; ++b)
         for (int a = 0; a <= N - d - b; ++a) put16(t->o_fstack, f * t->Np + q++, face_vol(N, f, a, b, d));
   }
+  for (int q = 0; q < t->Np; ++q) put16(t->o_sslot, q, stack_slot_of(N, q));
   std::vector<double> lj(N + 1, 0.0);
   std::vector<float> ljf(N + 1, 0.f);
   for (int j = 1; j <= N; ++j) {

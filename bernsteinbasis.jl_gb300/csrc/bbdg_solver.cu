@@ -147,6 +147,7 @@ int launch_fast(bb_solver* s, int mode, int stage, double dt, void* q, void* res
   P.o_node3m1 = t.o_node3m1;
   P.o_fvol = t.o_fvol;
   P.o_fperm = t.o_fperm;
+  P.o_sslot = t.o_sslot;
   P.K = s->K;
   P.mode = mode;
   P.rkA = float(mode ? kRK4A[stage] : 0.0);

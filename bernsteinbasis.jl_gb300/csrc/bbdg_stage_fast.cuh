@@ -5,7 +5,7 @@
 
 struct FastStageParams {
   const uint32_t* gtab;  // degree tables (DegTables::d_words) and their word offsets
-  int o_node3, o_node3m1, o_fvol, o_fperm;
+  int o_node3, o_node3m1, o_fvol, o_fperm, o_sslot;
   int64_t K;
   int mode;              // 0: rhs only, 1: LSRK stage update
   float rkA, rkB, dt, tau;

@@ -311,8 +311,10 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
         mb[b] = (uint32_t)(L::Z0 + zs);
       }
       // stack slots of this coefficient on faces f0 (i,k,j), f1 (j,k,l), f2 (j,k,i), f3 (i,j,k)
-      const uint32_t p0 = stack_slot<N>(ijk3(N, i, k, j)), p1 = stack_slot<N>(ijk3(N, j, k, l));
-      const uint32_t p2 = stack_slot<N>(ijk3(N, j, k, i)), p3 = stack_slot<N>(t);
+      // (the slot map is in the degree tables: no switch in the kernel's set-up code)
+      const uint16_t* gs = reinterpret_cast<const uint16_t*>(gw + P.o_sslot);
+      const uint32_t p0 = gs[ijk3(N, i, k, j)], p1 = gs[ijk3(N, j, k, l)];
+      const uint32_t p2 = gs[ijk3(N, j, k, i)], p3 = gs[t];
       // 10-bit fields: .x w indices of alpha - e_b for b = 0..2, .y stack slots on f0..f2,
       // .w stack slot on f3 and the w index for b = 3; .z alpha's barycentric indices
       // (i, j, k, l), one byte each
