@@ -303,6 +303,11 @@ def main():
                         "sample": f"{args.cpu_hex}^3 hexes x 6 tets (K={Ks}), N=9 FP32, "
                                   f"{args.cpu_steps} LSRK45 steps in {el:.1f} s, oracle port "
                                   f"(C++ restatement of the reference loops), OpenMP"}
+            # the same port on one thread (the reference itself is single-threaded)
+            r1, _, K1, el1 = cpu_port_rate(N_DEG, 8, 8, nthreads=1)
+            cpu_base["single_thread"] = {
+                "value": r1, "unit": "DOF-steps/s", "cores": 1,
+                "sample": f"8^3 hexes x 6 tets (K={K1}), N=9 FP32, 8 LSRK45 steps in {el1:.1f} s"}
         except Exception as exc:  # the baseline is reported, never required
             cpu_base = {"value": None, "unit": "DOF-steps/s", "cores": None, "kind": "port",
                         "sample": f"failed: {exc}"}
