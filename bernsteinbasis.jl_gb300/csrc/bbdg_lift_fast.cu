@@ -87,7 +87,11 @@ struct Lift4 {
   static constexpr int NFP = (N + 1) * (N + 2) / 2;
   static constexpr int NPS = NP | 1;    // stack stride: odd, conflict-free stack stores
   static constexpr int NFPP = NFP | 1;  // input row stride when staged from registers
-  static constexpr int EPW = 8;         // elements per warp: 32 chains
+  // elements per warp: 8 (32 chains) while the stacks leave room for several warps per SM;
+  // 4 (16 chains, half the lanes idle in the chain phase) from N = 11 on, which doubles the
+  // warps per SM for the loads and the gather (measured: N = 11 +16 %, N = 12 +17 %, N = 10
+  // -15 %)
+  static constexpr int EPW = N >= 11 ? 4 : 8;
   static constexpr int INW = EPW * 4 * NFP;  // input floats per tile
   // next tile in registers when they fit beside the chain, else a bulk copy
   static constexpr bool REG_PREFETCH = N <= 9;
@@ -95,10 +99,11 @@ struct Lift4 {
   // shared memory, bytes: [bulk input buffer][stacks (also the register-staged input)][perm]
   static constexpr int IN_B = REG_PREFETCH ? 0 : INW * 4;
   static constexpr int G_B = IN_B;
-  static constexpr int P_B = G_B + (32 * NPS * 4 + 15) / 16 * 16;
+  static constexpr int P_B = G_B + (EPW * 4 * NPS * 4 + 15) / 16 * 16;
   static constexpr int BAR_B = P_B + (NP * 4 + 15) / 16 * 16;
   static constexpr int SMEM = BAR_B + 16;
-  static_assert(32 * NFPP <= 32 * NPS, "staged inputs fit in the stack area");
+  static_assert(NFPP <= NPS, "staged inputs fit in the stack area");
+  static_assert(REG_PREFETCH ? EPW == 8 : true, "the register path stages 32 chains");
   static_assert(NP < 1024, "stack positions are packed in 10 bits");
   static_assert(INW % 4 == 0 && (INW * 4) % 16 == 0, "tiles are whole 16-byte chunks");
 };
@@ -206,7 +211,7 @@ __global__ void __launch_bounds__(32) lift4_kernel(int64_t K, const float* __res
       }
       ph ^= 1u;
 #pragma unroll
-      for (int m = 0; m < NFP; ++m) X[m] = sIn[t * NFP + m];
+      for (int m = 0; m < NFP; ++m) X[m] = sIn[(t < EPW * 4 ? t : 0) * NFP + m];
       __syncwarp();
       if (t == 0 && next < ntile) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
