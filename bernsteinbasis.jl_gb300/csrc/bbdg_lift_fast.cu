@@ -88,10 +88,10 @@ struct Lift4 {
   static constexpr int NPS = NP | 1;    // stack stride: odd, conflict-free stack stores
   static constexpr int NFPP = NFP | 1;  // input row stride when staged from registers
   // elements per warp: 8 (32 chains) while the stacks leave room for several warps per SM;
-  // 4 (16 chains, half the lanes idle in the chain phase) from N = 11 on, which doubles the
-  // warps per SM for the loads and the gather (measured: N = 11 +16 %, N = 12 +17 %, N = 10
-  // -15 %)
-  static constexpr int EPW = N >= 11 ? 4 : 8;
+  // 4 (16 chains, half the lanes idle in the chain phase) from N = 11 on and 2 from N = 13
+  // on, which keeps several warps per SM for the loads and the gather (measured at N = 11
+  // and 12: +16 %, +17 %; at N = 10 -15 %)
+  static constexpr int EPW = N >= 13 ? 2 : N >= 11 ? 4 : 8;
   static constexpr int INW = EPW * 4 * NFP;  // input floats per tile
   // next tile in registers when they fit beside the chain, else a bulk copy
   static constexpr bool REG_PREFETCH = N <= 9;
@@ -310,9 +310,10 @@ int launch_lift1(bb_ctx* ctx, int64_t K, const void* x, void* out, cudaStream_t 
 
 }  // namespace
 
-// FP32 lift of K columns with the degree-specialised kernels; nfaces 4 (BernsteinLift) or 1
-// (face_lift_multiply!). Returns -1 when no specialised kernel applies (degree above 12, or a
-// 4-face input or output that is not 16-byte aligned), and the caller runs the generic kernel.
+// FP32 lift of K columns with the degree-specialised kernels; nfaces 4 (BernsteinLift, N <= 15)
+// or 1 (face_lift_multiply!, N <= 12). Returns -1 when no specialised kernel applies (degree
+// above those, or a 4-face input or output that is not 16-byte aligned), and the caller runs
+// the generic kernel.
 int bb_lift_fast(bb_ctx* ctx, const DegTables* t, int64_t K, int nfaces, const void* x,
                  void* out, cudaStream_t st) {
   if (nfaces == 4 && ((((uintptr_t)x) | ((uintptr_t)out)) & 15) != 0) return -1;
@@ -321,9 +322,16 @@ int bb_lift_fast(bb_ctx* ctx, const DegTables* t, int64_t K, int nfaces, const v
     return nfaces == 4 ? launch_lift4<n_>(ctx, K, x, out, st)                      \
                        : launch_lift1<n_>(ctx, K, x, out, st);
   switch (t->N) {
-    // above N = 12 the register chains and the per-element stacks leave too few warps per SM
+    // the single-face kernel stops at N = 12 (its 32-element tiles leave too few warps per SM
+    // above); the level-parallel kernel runs it there
     BB_LF(1) BB_LF(2) BB_LF(3) BB_LF(4) BB_LF(5) BB_LF(6) BB_LF(7) BB_LF(8) BB_LF(9)
     BB_LF(10) BB_LF(11) BB_LF(12)
+    case 13:
+      return nfaces == 4 ? launch_lift4<13>(ctx, K, x, out, st) : -1;
+    case 14:
+      return nfaces == 4 ? launch_lift4<14>(ctx, K, x, out, st) : -1;
+    case 15:
+      return nfaces == 4 ? launch_lift4<15>(ctx, K, x, out, st) : -1;
     default:
       return -1;
   }

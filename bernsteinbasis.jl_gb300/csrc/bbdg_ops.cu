@@ -651,7 +651,7 @@ extern "C" int bb_fused_apply(bb_ctx* ctx, int N, int64_t K, int dtype, const vo
   const DegTables* t = bb_tables(ctx, N);
   if (!t) return bb_fail(ctx, BB_ERR_NOMEM, "table allocation failed");
   cudaStream_t st = (cudaStream_t)stream;
-  if (dtype == BB_F32 && N <= 12) {
+  if (dtype == BB_F32 && N <= 15) {
     // the gradient and lift calls back to back (degree-specialised kernels where they exist)
     // move the same bytes faster than the one-launch table-driven pass
     rc = launch_deriv<float>(ctx, t, K, 7, x, dr, ds, dt, st);

@@ -95,7 +95,7 @@ int bb_reduction_apply(bb_ctx* ctx, int N, int64_t K, int dtype, const void* x, 
                        void* stream);
 
 /* Fused operator pass: dr, ds, dt = D{r,s,t} x and lift = L faces (one launch; in FP32 with
- * N <= 12 the gradient and lift kernels back to back, whose results equal bb_grad_apply and
+ * N <= 15 the gradient and lift kernels back to back, whose results equal bb_grad_apply and
  * bb_lift_apply bitwise). */
 int bb_fused_apply(bb_ctx* ctx, int N, int64_t K, int dtype, const void* x,
                    const void* faces, void* dr, void* ds, void* dt, void* lift, void* stream);

@@ -101,12 +101,13 @@ def test_deriv_fp32_many_tiles_and_misaligned(cuda, bb, oracle_cpu, N):
     assert rel(om.cpu().numpy(), outs[1][:Km].cpu().numpy()) < TOL["f32"]
 
 
-@pytest.mark.parametrize("N", [3, 9, 10, 12])
+@pytest.mark.parametrize("N", [3, 9, 10, 11, 12, 13, 15])
 def test_lift_fp32_many_tiles_and_misaligned(cuda, bb, oracle_cpu, N):
-    """K = 20011 gives more 8-element tiles than the grid has blocks, so every block works
-    through several tiles (the register-prefetch path for N <= 9, the bulk-copy path above)
-    and ends on a ragged one; a sample of columns is checked against the oracle. Inputs and
-    outputs that are not 16-byte aligned take the generic kernel and agree with it."""
+    """K = 20011 gives more tiles (8, 4 or 2 elements) than the grid has blocks, so every
+    block works through several tiles (the register-prefetch path for N <= 9, the bulk-copy
+    path above) and ends on a ragged one; a sample of columns is checked against the oracle.
+    Inputs and outputs that are not 16-byte aligned take the generic kernel and agree with
+    it."""
     import torch
     rng = np.random.default_rng(90 + N)
     K = 20011
@@ -163,9 +164,9 @@ def test_fused_operator_pass(cuda, bb, N):
     assert torch.equal(li, ref[3])
 
 
-@pytest.mark.parametrize("N", [3, 9, 12])
+@pytest.mark.parametrize("N", [3, 9, 12, 15])
 def test_fused_operator_pass_fp32(cuda, bb, oracle_cpu, N):
-    """FP32 (N <= 12): the fused pass is the gradient and lift calls back to back and equals
+    """FP32 (N <= 15): the fused pass is the gradient and lift calls back to back and equals
     them bitwise; it matches the oracle at 1e-5."""
     import torch
     rng = np.random.default_rng(95 + N)
