@@ -99,6 +99,12 @@ struct FastLayout {
   static constexpr int TF_B = (FNB_B + 24 * NFP * 2 + 15) / 16 * 16;   // [NP] u32 face nodes
   static constexpr int BAR_B = (TF_B + NP * 4 + 15) / 16 * 16;         // 3 mbarriers
   static constexpr int BYTES = BAR_B + 32;
+  // element groups for the named-barrier hand-offs between the chain warps and the element
+  // threads: GS elements per group, NG groups, two barriers per group (ids 1..2 NG)
+  static constexpr int GS = EPB <= 7 ? 1 : (EPB + 6) / 7;
+  static constexpr int NG = EPB / GS;
+  static constexpr int GCOUNT = GS * TPE + CHT;  // threads at each hand-off
+  static_assert(EPB % GS == 0 && 2 * NG <= 15, "named barriers 1..15 cover the groups");
   // resident blocks per SM the register budget is sized for (2 when two tiles fit in the
   // shared memory of an SM, else 1)
   static constexpr int MINB = 2 * BYTES <= 227 * 1024 ? 2 : 1;
@@ -128,6 +134,15 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
       : "r"(s_addr(bar)), "r"(parity)
       : "memory");
   return ok != 0;
+}
+// Named hardware barriers (ids 1..15; id 0 is __syncthreads): bar.sync waits until `count`
+// threads have arrived, bar.arrive counts the caller without waiting. Both are executed by
+// whole warps.
+__device__ __forceinline__ void nbar_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+__device__ __forceinline__ void nbar_arrive(int id, int count) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
 // Bounded wait for the phase with the given parity: about a second at most, then false.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
@@ -347,12 +362,16 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
     }
   }
   __syncthreads();
-  // the first two tiles of this block go to the two slots
+  // the first two tiles of this block go to the two slots; the first chain thread issues
+  // every bulk copy and counts them per barrier (for the drain at the end)
   const int64_t t0 = blockIdx.x;
-  if (tid == 0 && t0 < ntiles) {
+  const bool issuer = tid == NTE;
+  uint32_t iss0 = 0u, iss1 = 0u, iss2 = 0u;
+  if (issuer && t0 < ntiles) {
     issue_main(t0, 0);
-    if (stage) issue_res(t0);
-    if (t0 + gridDim.x < ntiles) issue_main(t0 + gridDim.x, 1);
+    ++iss0;
+    if (stage) issue_res(t0), ++iss2;
+    if (t0 + gridDim.x < ntiles) issue_main(t0 + gridDim.x, 1), ++iss1;
   }
   uint32_t ph = 0u;  // bit b: parity of the phase barrier b waits for next (element threads)
   const float rkA = P.rkA, rkB = P.rkB, dt = P.dt, tau = P.tau;
@@ -434,14 +453,28 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
 
   // prologue: flux of the first tile
   if (is_elem && t0 < ntiles) {
-    if (!mbar_wait(&bar[0], 0u)) s_fail = 1;
+    if (!mbar_wait(&bar[0], 0u)) {
+      s_fail = 1;
+      atomicOr(P.status, 2);
+    }
     ph ^= 1u;
     flux_tile(t0, 0, sX);
   }
   __syncthreads();
 
+  // Hand-offs per tile (every thread runs the same barrier sequence in every iteration, also
+  // after a failure, when the work is skipped; so no barrier can wait for a thread that left):
+  //   B->A, at the start of tile i > 0: each element group's threads and the chain warps sync
+  //     on the group's barrier 1 + NG + g: the group has finished tile i-1 (its w may be
+  //     rewritten), and once the chain warps have passed all groups, the stacks, slot s^1 and
+  //     the res buffer are free and tile i's chain inputs are written;
+  //   A->B: the chain warps arrive on barrier 1 + g after the lifts of tile i, the group's
+  //     threads sync on it after forming w and the next tile's flux.
+  constexpr int GCOUNT = L::GCOUNT, NG = L::NG;
+  const int grp = le / L::GS;
+  volatile int* vfail = &s_fail;
   int it = 0;
-  for (int64_t tile = t0; tile < ntiles && !s_fail; tile += gridDim.x, ++it) {
+  for (int64_t tile = t0; tile < ntiles; tile += gridDim.x, ++it) {
     const int s = it & 1;
     const int64_t e0 = tile * EPB;
     const int64_t tnext = tile + gridDim.x;
@@ -452,8 +485,24 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
     // ---- A. chain warps: lift chains of this tile || element threads: volume term of
     //         this tile, then the interface flux of the next tile -------------------------
     if (!is_elem) {
+      if (it > 0) {
+        for (int g = 0; g < NG; ++g) nbar_sync(1 + NG + g, GCOUNT);
+        if (issuer && !*vfail && (tnext < ntiles || stage)) {
+          fence_async_smem();  // order the generic-proxy reads before the copies
+          if (tnext < ntiles) {
+            issue_main(tnext, s ^ 1);
+            if (s) ++iss0;
+            else ++iss1;
+          }
+          if (stage) issue_res(tile), ++iss2;
+        }
+      }
       const int c = tid - NTE;
-      if (c < NCHAIN) lift_chain<N, NCH>(sX + (s * NCHAIN + c) * NFP, sG + (c / NCH) * NPS * NCH + c % NCH);
+      if (!*vfail && c < NCHAIN)
+        lift_chain<N, NCH>(sX + (s * NCHAIN + c) * NFP, sG + (c / NCH) * NPS * NCH + c % NCH);
+      for (int g = 0; g < NG; ++g) nbar_arrive(1 + g, GCOUNT);
+    } else if (it > 0 && (nbar_sync(1 + NG + grp, GCOUNT), *vfail)) {
+      // a wait ran out: keep to the barrier sequence, skip the work
     } else {
       // the tile after next: its outside-tile neighbour traces (one contiguous NF x Nfp block
       // per face) are pulled into L2 now, a whole tile ahead of its flux phase
@@ -534,20 +583,25 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
         }
       }
       if (tnext < ntiles) {
-        if (!mbar_wait(&bar[s ^ 1], (ph >> (s ^ 1)) & 1u)) s_fail = 1;
+        if (!mbar_wait(&bar[s ^ 1], (ph >> (s ^ 1)) & 1u)) {
+          s_fail = 1;
+          atomicOr(P.status, 2);
+        }
         ph ^= 1u << (s ^ 1);
-        flux_tile(tnext, s ^ 1, sX + (s ^ 1) * NCHAIN * NFP);
+        if (!*vfail) flux_tile(tnext, s ^ 1, sX + (s ^ 1) * NCHAIN * NFP);
       }
-      if (stage) {
-        if (!mbar_wait(&bar[2], (ph >> 2) & 1u)) s_fail = 1;
+      if (stage && !*vfail) {
+        if (!mbar_wait(&bar[2], (ph >> 2) & 1u)) {
+          s_fail = 1;
+          atomicOr(P.status, 2);
+        }
         ph ^= 4u;
       }
     }
-    __syncthreads();
-    if (s_fail) break;
+    if (is_elem) nbar_sync(1 + grp, GCOUNT);
 
     // ---- B. sum lift stacks + volume term, divide by J, LSRK update ------------------
-    if (is_elem) {
+    if (is_elem && !*vfail) {
       const float* g = sGeo + le * BB_GEO_STRIDE;
       const float invJ = g[9];
       float nxf[4], nyf[4], nzf[4];
@@ -692,22 +746,13 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
         }
       }
     }
-    __syncthreads();
-    // the slot and the res buffer are free: fetch the tile after next into this slot and the
-    // next tile's res, both well ahead of their use
-    if (tid == 0) {
-      const int64_t tnn = tnext + gridDim.x;
-      if (tnn < ntiles || (stage && tnext < ntiles)) {
-        fence_async_smem();  // order the generic-proxy reads before the copies
-        if (tnn < ntiles) issue_main(tnn, s);
-        if (stage && tnext < ntiles) issue_res(tnext);
-      }
-    }
   }
-  if (s_fail && tid == 0) {
-    atomicOr(P.status, 2);
-    // let copies still in flight land before the block exits (bounded)
-    for (int b = 0; b < 3; ++b) mbar_wait(&bar[b], (ph >> b) & 1u);
+  if (issuer) {
+    // let the copies this thread issued land before the block exits: immediate when the
+    // element threads consumed them, bounded otherwise
+    if (iss0) mbar_wait(&bar[0], (iss0 - 1u) & 1u);
+    if (iss1) mbar_wait(&bar[1], (iss1 - 1u) & 1u);
+    if (iss2) mbar_wait(&bar[2], (iss2 - 1u) & 1u);
   }
 }
 
