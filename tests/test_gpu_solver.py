@@ -161,6 +161,21 @@ def test_corrupt_connectivity_is_reported(cuda, bb):
     assert ei.value.status == 7
 
 
+def test_corrupt_connectivity_is_reported_by_the_specialised_kernel(cuda, bb):
+    """The degree-specialised FP32 kernel checks every neighbour index before any access:
+    one out of range is skipped, flagged and reported as BB_ERR_DEVICE."""
+    import torch
+    from bbdg import BBError
+    m = bb.uniform_tet_mesh(2)                     # K = 48, a multiple of the N=9 tile
+    m.conn = m.conn.copy()
+    m.conn[5, 2] = np.int32((m.K + 9) << 5)        # neighbour index out of range
+    s = bb.DGSolver(m, 9, "wave", dtype=torch.float32, tau=1.0)
+    assert s.kernel == "specialised"
+    with pytest.raises(BBError) as ei:
+        s.rhs(s.zeros())
+    assert ei.value.status == 7
+
+
 FAST_TILES = {("wave", 9): [(4, 288), (4, 160), (2, 160)],
               ("maxwell", 9): [(2, 192), (2, 256)],
               ("wave", 5): [(4, 160), (8, 320), (2, 96)],
