@@ -79,11 +79,7 @@ __global__ void __launch_bounds__(kBatchThreads, 3)
     const int64_t item = s_item;
     if (item >= total) break;
     uint32_t* stab = reinterpret_cast<uint32_t*>(smem + sL.tab_bytes);
-    if (s_reload) {
-      load_tables(sP.tab, sP.gtab, stab);
-      T* sLj = reinterpret_cast<T*>(smem) + sL.lj;
-      for (int j = threadIdx.x; j <= sP.tab.N; j += blockDim.x) sLj[j] = sP.lj[j];
-    }
+    if (s_reload) load_tables(sP.tab, sP.gtab, stab);
     const SmemTables st = tables_view(sP.tab, stab);
     if (s_phys == BB_WAVE)
       generic_stage_tile<T, BB_WAVE>(sP, sL, st, item - s_begin);  // starts with a barrier
@@ -185,7 +181,6 @@ int build_desc(bb_batch* b) {
     memset(&d, 0, sizeof(d));
     d.P.tab = *t;
     d.P.gtab = t->d_words;
-    d.P.lj = sizeof(T) == 8 ? (const T*)t->d_lj : (const T*)t->d_ljf;
     d.P.K = pr.K;
     d.P.epb = b->epb[p];
     d.P.mode = 1;

@@ -74,8 +74,6 @@ struct DegTables {
   int o_sslot = 0;   // Np uint16: stage-kernel stack slot of lift-stack entry q (stack_slot<N>)
   int nwords = 0;
   uint32_t* d_words = nullptr;
-  double* d_lj = nullptr;  // N+1 entries, d_lj[j] = l_j(N) (constants.jl:10-12), [0] = 0
-  float* d_ljf = nullptr;
 };
 
 // Orientation codes: face vertex m of this side is face vertex PERMS[o][m] of the partner,
@@ -226,47 +224,113 @@ __host__ __device__ __forceinline__ size_t align16(size_t x) { return (x + 15) &
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 
+// Small non-negative integers (0 <= v < 2^21) and reciprocals 1/n (1 <= n <= BB_MAX_DEGREE + 1)
+// as T, with the values T(v) and T(1) / T(n) give. In double both stay off the FP64 pipe,
+// GB300's scarcest unit (about 1 TFLOP/s), which a conversion or a division would otherwise
+// occupy like the arithmetic: the integer is assembled in the binary64 fields with integer
+// instructions (for v in [2^e, 2^(e+1)): biased exponent 1023 + e and the e bits below the
+// leading one at the top of the fraction, exact since e <= 20), and 1/n is read from a table
+// whose entries the compiler rounds as the IEEE division does. In float the plain
+// conversion and division stay.
+template <class T>
+__device__ __forceinline__ T small_int(int v) {
+  return T(v);
+}
+template <>
+__device__ __forceinline__ double small_int<double>(int v) {
+  const int e = 31 - __clz(v | 1);
+  const uint32_t hi = ((uint32_t)(1023 + e) << 20) | (((uint32_t)v << (20 - e)) & 0xFFFFFu);
+  return __hiloint2double(v ? (int)hi : 0, 0);
+}
+static __constant__ double kInvInt[BB_MAX_DEGREE + 2] = {
+    0.0,       1.0 / 1,  1.0 / 2,  1.0 / 3,  1.0 / 4,  1.0 / 5,  1.0 / 6,  1.0 / 7,
+    1.0 / 8,   1.0 / 9,  1.0 / 10, 1.0 / 11, 1.0 / 12, 1.0 / 13, 1.0 / 14, 1.0 / 15,
+    1.0 / 16,  1.0 / 17, 1.0 / 18, 1.0 / 19, 1.0 / 20, 1.0 / 21};
+static_assert(BB_MAX_DEGREE + 2 == 22, "kInvInt lists 1/n for n = 1 .. BB_MAX_DEGREE + 1");
+template <class T>
+__device__ __forceinline__ T inv_int(int n) {
+  return T(1) / T(n);
+}
+template <>
+__device__ __forceinline__ double inv_int<double>(int n) {
+  return kInvInt[n];
+}
+// v / 2 for 0 <= v < 2^21 (double only): the fields of small_int with the exponent one lower.
+__device__ __forceinline__ double half_int_f64(int v) {
+  const int e = 31 - __clz(v | 1);
+  const uint32_t hi = ((uint32_t)(1022 + e) << 20) | (((uint32_t)v << (20 - e)) & 0xFFFFFu);
+  return __hiloint2double(v ? (int)hi : 0, 0);
+}
+
 // L0 x at face node (i, j) of degree N, k = N - i - j: the 7-point stencil of
 // (N+1)^2/2 R_{N+1} E_{N->N+1} (src/BernsteinLift.jl:100-125 then :66-90 with the L0
 // scaling), x in the 2D layout of degree N with row offsets rb (row j), rbn (row j+1) and
-// rbp (row j-1). Shared by the level-parallel and the chain-per-thread lifts so that both
-// give the same bits.
+// rbp (row j-1). Shared by the level-parallel and the chain-per-thread lifts. In double the
+// halving is folded into the stencil weights (c/2 instead of a final product by 1/2): every
+// partial sum is then exactly half of the unhalved one, so the bits are the same and the
+// FP64 pipe does one product less per point.
 template <class T>
 __device__ __forceinline__ T l0_point(int i, int j, int k, const T* x, int rb, int rbn, int rbp) {
-  T v = T((i + 1) * (i + 1) + (j + 1) * (j + 1) + (k + 1) * (k + 1)) * x[rb + i];
-  if (j > 0) v = fma(T((i + 1) * j), x[rbp + i + 1], v);  // x(i+1, j-1)
-  if (k > 0) v = fma(T((i + 1) * k), x[rb + i + 1], v);   // x(i+1, j)
-  if (i > 0) v = fma(T((j + 1) * i), x[rbn + i - 1], v);  // x(i-1, j+1)
-  if (k > 0) v = fma(T((j + 1) * k), x[rbn + i], v);      // x(i, j+1)
-  if (i > 0) v = fma(T((k + 1) * i), x[rb + i - 1], v);   // x(i-1, j)
-  if (j > 0) v = fma(T((k + 1) * j), x[rbp + i], v);      // x(i, j-1)
-  return mul_rn(T(0.5), v);
+  constexpr bool H = sizeof(T) == 8;
+  auto c = [](int v) -> T {
+    if constexpr (H) return half_int_f64(v);
+    else return small_int<T>(v);
+  };
+  T v = c((i + 1) * (i + 1) + (j + 1) * (j + 1) + (k + 1) * (k + 1)) * x[rb + i];
+  if (j > 0) v = fma(c((i + 1) * j), x[rbp + i + 1], v);  // x(i+1, j-1)
+  if (k > 0) v = fma(c((i + 1) * k), x[rb + i + 1], v);   // x(i+1, j)
+  if (i > 0) v = fma(c((j + 1) * i), x[rbn + i - 1], v);  // x(i-1, j+1)
+  if (k > 0) v = fma(c((j + 1) * k), x[rbn + i], v);      // x(i, j+1)
+  if (i > 0) v = fma(c((k + 1) * i), x[rb + i - 1], v);   // x(i-1, j)
+  if (j > 0) v = fma(c((k + 1) * j), x[rbp + i], v);      // x(i, j-1)
+  if constexpr (H) return v;
+  else return mul_rn(T(0.5), v);
 }
 
-// reduction_multiply! (src/BernsteinLift.jl:81-85) at output (i, j) from degree n:
-// ((i+1) x(i+1,j) + (j+1) x(i,j+1) + (n-i-j) x(i,j)) / n.
+// reduction_multiply! (src/BernsteinLift.jl:81-85) at output (i, j) from degree n, times a
+// scale: ((i+1) x(i+1,j) + (j+1) x(i,j+1) + (n-i-j) x(i,j)) * scale (scale = 1/n is the
+// reference's step; the lifts pass l_d / (l_{d-1} n) = -1/(d+1) to carry the layer weights).
 template <class T>
-__device__ __forceinline__ T reduce_point(int i, int j, int n, T x_ip, T x_jp, T x_0, T inv) {
-  return fma(T(i + 1), x_ip, fma(T(j + 1), x_jp, T(n - i - j) * x_0)) * inv;
+__device__ __forceinline__ T reduce_point(int i, int j, int n, T x_ip, T x_jp, T x_0, T scale) {
+  return fma(small_int<T>(i + 1), x_ip, fma(small_int<T>(j + 1), x_jp, small_int<T>(n - i - j) * x_0)) *
+         scale;
 }
 
 // One face's recursive lift, accumulated into a shared-memory volume block, for `ne`
 // elements and `nfld` fields at once (src/BernsteinLift.jl:139-164 applied per face and
 // summed through the permutations of :207-218):
-//   layer 0 += E_0 = L0 x (7-point stencil);  E_d = R_{N-d+1} E_{d-1};  layer d += l_d E_d
+//   layer 0 += F_0 = L0 x (7-point stencil);  layer d += F_d = l_d E_d, E_d = R_{N-d+1} E_{d-1}
+// with l_d carried by the recursion: l_d / l_{d-1} = -(N-d+1)/(d+1) and R_n divides by
+// n = N-d+1, so F_d = -1/(d+1) [(i+1) F_{d-1}(i+1,j) + (j+1) F_{d-1}(i,j+1) + (n-i-j) F_{d-1}(i,j)]
+// and no product by l_d is left per point.
 // Level-parallel: one thread per output coefficient, a block barrier between levels, and
 // two ping-pong buffers (the reference's in-place reduction is not parallel-safe).
 //   in(le, fld)  : Nfp face coefficients at in + (le*in_es + fld*in_fs)
 //   out(le, fld) : Np volume coefficients at out + (le*out_es + fld*out_fs)
 //   bufA/bufB    : ne*nfld*np2(N) scratch each
+// WAVE_N (the wave stage, nfld = 2): chain 0 lifts the pressure flux into out field 0 and
+// chain 1 the scalar velocity flux s, whose lift goes to out fields 1, 2, 3 times this face's
+// normal (nrm[le*BB_GEO_STRIDE + 0 / 4 / 8] = nx, ny, nz): the velocity flux is s n and
+// the lift is linear, so one chain serves the three components.
 // All threads of the block must call it.
-template <class T>
+template <class T, bool WAVE_N = false>
 __device__ void lift_face_accumulate(int N, int f, int ne, int nfld, const uint16_t* node2,
                                      const T* in, int in_es, int in_fs, T* out, int out_es,
-                                     int out_fs, T* bufA, T* bufB, const T* lj) {
+                                     int out_fs, T* bufA, T* bufB, const T* nrm = nullptr) {
   const int S = np2(N);
   const int nchain = ne * nfld;
   const FastDiv by_nfld(nfld);
+  auto add = [&](int le, int fld, int v, T val) {
+    T* o = out + le * out_es + fld * out_fs + v;
+    if (WAVE_N && fld == 1) {
+      const T* g = nrm + le * BB_GEO_STRIDE;
+      o[0] = fma(g[0], val, o[0]);
+      o[out_fs] = fma(g[4], val, o[out_fs]);
+      o[2 * out_fs] = fma(g[8], val, o[2 * out_fs]);
+    } else {
+      o[0] += val;
+    }
+  };
   // level 0: the L0 stencil on the degree-N face values
   {
     const uint16_t* dec = node2 + np3(N - 1);
@@ -279,8 +343,7 @@ __device__ void lift_face_accumulate(int N, int f, int ne, int nfld, const uint1
       const int rb = tri_off(N, b);
       const T e = l0_point<T>(a, b, c, x, rb, rb + (N + 1 - b), rb - (N + 2 - b));
       bufA[ch * S + m] = e;
-      T* o = out + le * out_es + fld * out_fs;
-      o[face_vol(N, f, a, b, 0)] += e;
+      add(le, fld, face_vol(N, f, a, b, 0), e);
     }
   }
   __syncthreads();
@@ -290,8 +353,7 @@ __device__ void lift_face_accumulate(int N, int f, int ne, int nfld, const uint1
     const int n = N + 1 - d;         // input degree
     const int cnt = np2(n - 1);      // outputs
     const uint16_t* dec = node2 + np3(n - 2);
-    const T inv = T(1) / T(n);
-    const T wl = lj[d];
+    const T cd = -inv_int<T>(d + 1);  // l_d / (l_{d-1} n)
     const FastDiv by_cnt(cnt);
     for (int it = threadIdx.x; it < nchain * cnt; it += blockDim.x) {
       const int ch = by_cnt.div(it), m = it - ch * cnt;
@@ -299,10 +361,9 @@ __device__ void lift_face_accumulate(int N, int f, int ne, int nfld, const uint1
       const int a = dec[m] & 0xff, b = dec[m] >> 8;
       const T* x = src + ch * S;
       const T val = reduce_point<T>(a, b, n, x[ij2(n, a + 1, b)], x[ij2(n, a, b + 1)],
-                                    x[ij2(n, a, b)], inv);
+                                    x[ij2(n, a, b)], cd);
       dst[ch * S + m] = val;
-      T* o = out + le * out_es + fld * out_fs;
-      o[face_vol(N, f, a, b, d)] += mul_rn(wl, val);
+      add(le, fld, face_vol(N, f, a, b, d), val);
     }
     __syncthreads();
     T* tmp = src;

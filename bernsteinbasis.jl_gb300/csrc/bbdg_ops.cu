@@ -64,8 +64,6 @@ extern "C" int bb_ctx_create(int device, bb_ctx** out) {
 static void free_tables(DegTables* t) {
   if (!t) return;
   cudaFree(t->d_words);
-  cudaFree(t->d_lj);
-  cudaFree(t->d_ljf);
   delete t;
 }
 
@@ -94,12 +92,6 @@ static int stack_slot_of(int N, int q) {
     case 10: return stack_slot<10>(q);
     default: return q;
   }
-}
-
-static double lift_lj(int N, int j) {
-  double b = 1.0;
-  for (int m = 1; m <= j; ++m) b = b * (N - j + m) / m;
-  return ((j % 2) ? -1.0 : 1.0) * b / (1.0 + j);
 }
 
 const DegTables* bb_tables(bb_ctx* ctx, int N) {
@@ -163,20 +155,10 @@ const DegTables* bb_tables(bb_ctx* ctx, int N) {
         for (int a = 0; a <= N - d - b; ++a) put16(t->o_fstack, f * t->Np + q++, face_vol(N, f, a, b, d));
   }
   for (int q = 0; q < t->Np; ++q) put16(t->o_sslot, q, stack_slot_of(N, q));
-  std::vector<double> lj(N + 1, 0.0);
-  std::vector<float> ljf(N + 1, 0.f);
-  for (int j = 1; j <= N; ++j) {
-    lj[j] = lift_lj(N, j);
-    ljf[j] = (float)lj[j];
-  }
+  // (the lift weights l_j(N), constants.jl:10-12, are carried by the chain recursion:
+  // no table of them is needed)
   bool ok = cudaMalloc(&t->d_words, sizeof(uint32_t) * off) == cudaSuccess &&
-            cudaMalloc(&t->d_lj, sizeof(double) * (N + 1)) == cudaSuccess &&
-            cudaMalloc(&t->d_ljf, sizeof(float) * (N + 1)) == cudaSuccess &&
             cudaMemcpy(t->d_words, w.data(), sizeof(uint32_t) * off, cudaMemcpyHostToDevice) ==
-                cudaSuccess &&
-            cudaMemcpy(t->d_lj, lj.data(), sizeof(double) * (N + 1), cudaMemcpyHostToDevice) ==
-                cudaSuccess &&
-            cudaMemcpy(t->d_ljf, ljf.data(), sizeof(float) * (N + 1), cudaMemcpyHostToDevice) ==
                 cudaSuccess;
   if (!ok) {
     free_tables(t);
@@ -198,27 +180,27 @@ __device__ __forceinline__ T deriv_row(int axis, int N, const T* x, int i, int j
   T val;
   if (axis == 0) {  // BernsteinDerivativeMatrix_3D.jl:96-132
     T x4 = (i > 0) ? x[ijk3(N, i - 1, j, k)] : T(0);
-    val = T(i) * (xr - x4);
-    if (j > 0) val += T(j) * (x[ijk3(N, i + 1, j - 1, k)] - x[ijk3(N, i, j - 1, k)]);
-    if (k > 0) val += T(k) * (x[ijk3(N, i + 1, j, k - 1)] - x[ijk3(N, i, j, k - 1)]);
+    val = small_int<T>(i) * (xr - x4);
+    if (j > 0) val += small_int<T>(j) * (x[ijk3(N, i + 1, j - 1, k)] - x[ijk3(N, i, j - 1, k)]);
+    if (k > 0) val += small_int<T>(k) * (x[ijk3(N, i + 1, j, k - 1)] - x[ijk3(N, i, j, k - 1)]);
     T x1 = (l > 0) ? x[ijk3(N, i + 1, j, k)] : T(0);
-    val += T(l) * (x1 - xr);
+    val += small_int<T>(l) * (x1 - xr);
   } else if (axis == 1) {  // :138-174
     val = T(0);
-    if (i > 0) val = T(i) * (x[ijk3(N, i - 1, j + 1, k)] - x[ijk3(N, i - 1, j, k)]);
+    if (i > 0) val = small_int<T>(i) * (x[ijk3(N, i - 1, j + 1, k)] - x[ijk3(N, i - 1, j, k)]);
     T x4 = (j > 0) ? x[ijk3(N, i, j - 1, k)] : T(0);
-    val += T(j) * (xr - x4);
-    if (k > 0) val += T(k) * (x[ijk3(N, i, j + 1, k - 1)] - x[ijk3(N, i, j, k - 1)]);
+    val += small_int<T>(j) * (xr - x4);
+    if (k > 0) val += small_int<T>(k) * (x[ijk3(N, i, j + 1, k - 1)] - x[ijk3(N, i, j, k - 1)]);
     T x2 = (l > 0) ? x[ijk3(N, i, j + 1, k)] : T(0);
-    val += T(l) * (x2 - xr);
+    val += small_int<T>(l) * (x2 - xr);
   } else {  // :180-216
     val = T(0);
-    if (i > 0) val = T(i) * (x[ijk3(N, i - 1, j, k + 1)] - x[ijk3(N, i - 1, j, k)]);
-    if (j > 0) val += T(j) * (x[ijk3(N, i, j - 1, k + 1)] - x[ijk3(N, i, j - 1, k)]);
+    if (i > 0) val = small_int<T>(i) * (x[ijk3(N, i - 1, j, k + 1)] - x[ijk3(N, i - 1, j, k)]);
+    if (j > 0) val += small_int<T>(j) * (x[ijk3(N, i, j - 1, k + 1)] - x[ijk3(N, i, j - 1, k)]);
     T x4 = (k > 0) ? x[ijk3(N, i, j, k - 1)] : T(0);
-    val += T(k) * (xr - x4);
+    val += small_int<T>(k) * (xr - x4);
     T x3 = (l > 0) ? x[ijk3(N, i, j, k + 1)] : T(0);
-    val += T(l) * (x3 - xr);
+    val += small_int<T>(l) * (x3 - xr);
   }
   return T(0.5) * val;
 }
@@ -317,8 +299,8 @@ __global__ void __launch_bounds__(256) deriv_fact_kernel(DegTables tab,
       const uint2 ga = sGA[n];
       const uint32_t gw = sGW[n];
       const int m0 = ga.x & 0xffff, m1 = ga.x >> 16, m2 = ga.y & 0xffff, m3 = ga.y >> 16;
-      const T a0 = T(gw & 0xff), a1 = T((gw >> 8) & 0xff), a2 = T((gw >> 16) & 0xff),
-              a3 = T(gw >> 24);
+      const T a0 = small_int<T>(gw & 0xff), a1 = small_int<T>((gw >> 8) & 0xff),
+              a2 = small_int<T>((gw >> 16) & 0xff), a3 = small_int<T>(gw >> 24);
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
         if (!(mask & (1 << a))) continue;
@@ -336,7 +318,7 @@ __global__ void __launch_bounds__(256) deriv_fact_kernel(DegTables tab,
 // directly, src/BernsteinLift.jl:139-164) of EPB element columns per block iteration.
 template <class T>
 __global__ void __launch_bounds__(256) lift_kernel(DegTables tab, const uint32_t* __restrict__ gtab,
-                                                   const T* __restrict__ lj_g, int64_t K, int epb,
+                                                   int64_t K, int epb,
                                                    int nfaces, const T* __restrict__ x,
                                                    T* __restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -347,11 +329,9 @@ __global__ void __launch_bounds__(256) lift_kernel(DegTables tab, const uint32_t
   T* sout = sin + epb * in_cols;
   T* bufA = sout + epb * Np;
   T* bufB = bufA + epb * S;
-  T* slj = bufB + epb * S;
   uint32_t* stab = reinterpret_cast<uint32_t*>(
-      smem + align16(sizeof(T) * ((size_t)epb * (in_cols + Np + 2 * S) + N + 1)));
+      smem + align16(sizeof(T) * ((size_t)epb * (in_cols + Np + 2 * S))));
   const SmemTables st = load_tables(tab, gtab, stab);
-  for (int j = threadIdx.x; j <= N; j += blockDim.x) slj[j] = lj_g[j];
   const int64_t nblk = (K + epb - 1) / epb;
   for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
     const int64_t e0 = blk * epb;
@@ -362,14 +342,13 @@ __global__ void __launch_bounds__(256) lift_kernel(DegTables tab, const uint32_t
     __syncthreads();
     if (nfaces == 4) {
       // face 4 (t = -1) first, then f1, f2, f3, as src/BernsteinLift.jl:202-218
-      const int order[4] = {3, 0, 1, 2};
       for (int q = 0; q < 4; ++q) {
-        const int f = order[q];
+        const int f = (q + 3) & 3;  // faces 3, 0, 1, 2
         lift_face_accumulate<T>(N, f, ne, 1, st.node2, sin + f * Nfp, in_cols, 0, sout, Np, 0,
-                                bufA, bufB, slj);
+                                bufA, bufB);
       }
     } else {
-      lift_face_accumulate<T>(N, 3, ne, 1, st.node2, sin, Nfp, 0, sout, Np, 0, bufA, bufB, slj);
+      lift_face_accumulate<T>(N, 3, ne, 1, st.node2, sin, Nfp, 0, sout, Np, 0, bufA, bufB);
     }
     copy_s2g(out + e0 * Np, sout, ne * Np);
   }
@@ -379,7 +358,7 @@ __global__ void __launch_bounds__(256) lift_kernel(DegTables tab, const uint32_t
 // of the same EPB elements, one launch, each input read once.
 template <class T>
 __global__ void __launch_bounds__(256) fused_kernel(DegTables tab, const uint32_t* __restrict__ gtab,
-                                                    const T* __restrict__ lj_g, int64_t K, int epb,
+                                                    int64_t K, int epb,
                                                     const T* __restrict__ x, const T* __restrict__ faces,
                                                     T* __restrict__ dr, T* __restrict__ ds,
                                                     T* __restrict__ dt, T* __restrict__ out) {
@@ -392,11 +371,9 @@ __global__ void __launch_bounds__(256) fused_kernel(DegTables tab, const uint32_
   T* sout = sin + epb * in_cols;
   T* bufA = sout + epb * Np;
   T* bufB = bufA + epb * S;
-  T* slj = bufB + epb * S;
   uint32_t* stab = reinterpret_cast<uint32_t*>(
-      smem + align16(sizeof(T) * ((size_t)epb * (Np + in_cols + Np + 2 * S) + N + 1)));
+      smem + align16(sizeof(T) * ((size_t)epb * (Np + in_cols + Np + 2 * S))));
   const SmemTables st = load_tables(tab, gtab, stab);
-  for (int j = threadIdx.x; j <= N; j += blockDim.x) slj[j] = lj_g[j];
   T* outs[3] = {dr, ds, dt};
   const int64_t nblk = (K + epb - 1) / epb;
   for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
@@ -414,11 +391,10 @@ __global__ void __launch_bounds__(256) fused_kernel(DegTables tab, const uint32_
 #pragma unroll
       for (int a = 0; a < 3; ++a) outs[a][e0 * Np + it] = deriv_row<T>(a, N, sx + le * Np, i, j, k, row);
     }
-    const int order[4] = {3, 0, 1, 2};
     for (int q = 0; q < 4; ++q) {
-      const int f = order[q];
+      const int f = (q + 3) & 3;  // faces 3, 0, 1, 2
       lift_face_accumulate<T>(N, f, ne, 1, st.node2, sin + f * Nfp, in_cols, 0, sout, Np, 0,
-                              bufA, bufB, slj);
+                              bufA, bufB);
     }
     copy_s2g(out + e0 * Np, sout, ne * Np);
   }
@@ -512,7 +488,7 @@ static int launch_lift(bb_ctx* ctx, const DegTables* t, int64_t K, int nfaces, c
   int epb = 8;
   size_t smem = 0;
   for (; epb >= 1; epb /= 2) {
-    smem = align16(sizeof(T) * ((size_t)epb * (nfaces * t->Nfp + t->Np + 2 * S) + t->N + 1)) +
+    smem = align16(sizeof(T) * ((size_t)epb * (nfaces * t->Nfp + t->Np + 2 * S))) +
            4 * (size_t)t->nwords;
     if (smem <= 64 * 1024) break;
   }
@@ -520,8 +496,7 @@ static int launch_lift(bb_ctx* ctx, const DegTables* t, int64_t K, int nfaces, c
   BB_CUDA(ctx, cudaFuncSetAttribute(lift_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem));
   const int64_t nblk = (K + epb - 1) / epb;
-  const T* lj = sizeof(T) == 8 ? (const T*)t->d_lj : (const T*)t->d_ljf;
-  lift_kernel<T><<<grid_for(ctx, nblk, 4), 256, smem, st>>>(*t, t->d_words, lj, K, epb, nfaces,
+  lift_kernel<T><<<grid_for(ctx, nblk, 4), 256, smem, st>>>(*t, t->d_words, K, epb, nfaces,
                                                              (const T*)x, (T*)out);
   return bb_check_launch(ctx, "lift_kernel");
 }
@@ -533,7 +508,7 @@ static int launch_fused(bb_ctx* ctx, const DegTables* t, int64_t K, const void* 
   int epb = 8;
   size_t smem = 0;
   for (; epb >= 1; epb /= 2) {
-    smem = align16(sizeof(T) * ((size_t)epb * (2 * t->Np + 4 * t->Nfp + 2 * S) + t->N + 1)) +
+    smem = align16(sizeof(T) * ((size_t)epb * (2 * t->Np + 4 * t->Nfp + 2 * S))) +
            4 * (size_t)t->nwords;
     if (smem <= 64 * 1024) break;
   }
@@ -541,8 +516,7 @@ static int launch_fused(bb_ctx* ctx, const DegTables* t, int64_t K, const void* 
   BB_CUDA(ctx, cudaFuncSetAttribute(fused_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem));
   const int64_t nblk = (K + epb - 1) / epb;
-  const T* lj = sizeof(T) == 8 ? (const T*)t->d_lj : (const T*)t->d_ljf;
-  fused_kernel<T><<<grid_for(ctx, nblk, 4), 256, smem, st>>>(*t, t->d_words, lj, K, epb, (const T*)x,
+  fused_kernel<T><<<grid_for(ctx, nblk, 4), 256, smem, st>>>(*t, t->d_words, K, epb, (const T*)x,
                                                               (const T*)faces, (T*)dr, (T*)ds,
                                                               (T*)dt, (T*)out);
   return bb_check_launch(ctx, "fused_kernel");

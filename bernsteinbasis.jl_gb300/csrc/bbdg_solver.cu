@@ -18,8 +18,6 @@ __global__ void __launch_bounds__(kThreads) stage_kernel(StageParams<T> P, TileL
   extern __shared__ __align__(16) unsigned char smem[];
   const SmemTables st =
       load_tables(P.tab, P.gtab, reinterpret_cast<uint32_t*>(smem + L.tab_bytes));
-  T* sLj = reinterpret_cast<T*>(smem) + L.lj;
-  for (int j = threadIdx.x; j <= P.tab.N; j += blockDim.x) sLj[j] = P.lj[j];
   const int64_t ntiles = (P.K + P.epb - 1) / P.epb;
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
     generic_stage_tile<T, PHYS>(P, L, st, tile);
@@ -107,7 +105,6 @@ int launch_stage_t(bb_solver* s, int mode, int stage, double dt, void* q, void* 
   StageParams<T> P;
   P.tab = *s->tab;
   P.gtab = s->tab->d_words;
-  P.lj = sizeof(T) == 8 ? (const T*)s->tab->d_lj : (const T*)s->tab->d_ljf;
   P.K = s->K;
   P.epb = s->epb;
   P.mode = mode;
@@ -292,10 +289,9 @@ extern "C" int bb_solver_create(bb_ctx* ctx, int physics, int N, int64_t K, int 
   s->geo = geo;
   s->tau = tau;
   s->tab = t;
-  // default tile: the largest of 12, 6, 4, 2 elements whose tile runs the chain lift (fits
-  // in its shared-memory budget); else, in this order, 4, 2, 6, 12 or 1 elements within
-  // 100 KB (a one-element chain tile ran 1.5x slower than four-element level-parallel
-  // tiles in FP64 at N = 9)
+  // default tile: the largest of 12, 6, 4, 2 elements whose tile runs the chain lift (FP32
+  // tiles that fit its shared-memory budget); else, in this order, 4, 2, 6, 12 or 1 elements
+  // within 100 KB (FP64 always lifts level-parallel: wave N = 9 takes 2 elements)
   const int cands[2][5] = {{12, 6, 4, 2, 0}, {4, 2, 6, 12, 1}};
   for (int pass = 0; pass < 2 && !s->epb; ++pass)
     for (int c : cands[pass]) {

@@ -24,12 +24,14 @@ template <>
 struct Phys<BB_WAVE> {
   static constexpr int NF = 4;  // p, u, v, w
   static constexpr int NW = 4;  // div(u,v,w), dp/dx, dp/dy, dp/dz (scaled by J)
+  static constexpr int NCH = 2;  // lift chains per face: pressure flux, scalar velocity flux
   static constexpr float vol_sign = -1.f;
 };
 template <>
 struct Phys<BB_MAXWELL> {
   static constexpr int NF = 6;  // Hx, Hy, Hz, Ex, Ey, Ez
   static constexpr int NW = 6;  // curl terms
+  static constexpr int NCH = 6;  // one lift chain per field
   static constexpr float vol_sign = 1.f;
 };
 // examples/3d_advec_scalar.jl: du = -(LIFT flux + J du/dx) / J; the flux is stored negated
@@ -38,6 +40,7 @@ template <>
 struct Phys<BB_ADVECTION> {
   static constexpr int NF = 1;  // u
   static constexpr int NW = 1;  // J du/dx
+  static constexpr int NCH = 1;
   static constexpr float vol_sign = -1.f;
 };
 
@@ -45,7 +48,6 @@ template <class T>
 struct StageParams {
   DegTables tab;
   const uint32_t* gtab;
-  const T* lj;
   int64_t K;
   int epb;
   int mode;             // 0: write rhs to `rhs`; 1: LSRK stage update of q and res
@@ -64,7 +66,7 @@ struct StageParams {
 // thread per (element, face, field) chain with the face stacks in shared memory (used when
 // that fits in kChainLiftBytes); chain == 0: the level-parallel lift with two ping-pong rows.
 struct TileLayout {
-  size_t q, out, flux, work, geo, lj, conn_bytes, tab_bytes, total;
+  size_t q, out, flux, work, geo, conn_bytes, tab_bytes, total;
   int work_elems;
   int chain;
 };
@@ -73,24 +75,28 @@ constexpr size_t kChainLiftBytes = 100 * 1024;
 // size is chosen per physics and degree) runs the same code inside the batch.
 constexpr size_t kBatchChainLiftBytes = kChainLiftBytes;
 
+// Lift chains per face for NF fields (Phys<PHYS>::NCH): the wave's velocity flux is a scalar
+// times the face normal, so its three components share one chain.
+__host__ __device__ inline int lift_chains(int NF) { return NF == 4 ? 2 : NF; }
+
 // Layout for degree N with Np/Nfp/NpM1 coefficients, NF fields, NW volume terms, scalars of
 // `tsize` bytes and `nwords` 32-bit table words.
 __host__ __device__ inline TileLayout tile_layout_with(int N, int NF, int NW, size_t tsize,
                                                       int nwords, int epb, int chain) {
   TileLayout L;
   const size_t Np = np3(N), Nfp = np2(N), NpM1 = np3(N - 1), S = np2(N + 1);
+  const size_t nch = (size_t)lift_chains(NF);
   size_t off = 0;
   L.q = off; off += (size_t)NF * epb * Np;
   L.out = off; off += (size_t)NF * epb * Np;
   L.flux = off; off += (size_t)epb * 4 * NF * Nfp;
   L.work = off;
   const size_t wvol = (size_t)NW * epb * NpM1;
-  const size_t wlift = chain ? (size_t)epb * 4 * NF * (Np + (Nfp | 1))  // stacks + rows
-                             : 2 * (size_t)epb * NF * S;
+  const size_t wlift = chain ? (size_t)epb * 4 * nch * (Np + (Nfp | 1))  // stacks + rows
+                             : 2 * (size_t)epb * nch * S;
   L.work_elems = (int)(wvol > wlift ? wvol : wlift);
   off += L.work_elems;
   L.geo = off; off += (size_t)epb * BB_GEO_STRIDE;
-  L.lj = off; off += N + 1;
   size_t bytes = align16(off * tsize);
   L.conn_bytes = bytes; bytes += align16((size_t)epb * 4 * sizeof(int32_t));
   L.tab_bytes = bytes; bytes += (size_t)nwords * 4;
@@ -99,23 +105,28 @@ __host__ __device__ inline TileLayout tile_layout_with(int N, int NF, int NW, si
   return L;
 }
 
-// The chain lift when its tile fits in `budget` bytes, else the level-parallel one.
+// FP32: the chain lift when its tile fits in `budget` bytes, else the level-parallel one.
+// FP64 always takes the level-parallel lift: the chain phase keeps one thread per (element,
+// face, chain) busy, too few to feed the FP64 pipe (wave N = 9, 2-element tiles: the pipe is
+// 48 % busy with chains against 80 % level-parallel, 2.38 against 1.65 ms per stage).
 __host__ __device__ inline TileLayout tile_layout_for(int N, int NF, int NW, size_t tsize,
                                                      int nwords, int epb,
                                                      size_t budget = kChainLiftBytes) {
   const TileLayout c = tile_layout_with(N, NF, NW, tsize, nwords, epb, 1);
-  return c.total <= budget ? c : tile_layout_with(N, NF, NW, tsize, nwords, epb, 0);
+  return tsize == 4 && c.total <= budget ? c : tile_layout_with(N, NF, NW, tsize, nwords, epb, 0);
 }
 
 // One face lift chain for run-time N, one thread (src/BernsteinLift.jl:139-164):
-//   E_0 = L0 x (the 7-point stencil of (N+1)^2/2 R_{N+1} E_{N->N+1}), E_d = R_{N-d+1} E_{d-1}
-// in place in ascending order on the thread's shared-memory row E (degree-N layout), and
-// l_d E_d written to the face's stack g in volume order through the stack table fst
-// (face f's entries: layer d, then j, then i, i + j <= N - d).
+//   F_0 = L0 x (the 7-point stencil of (N+1)^2/2 R_{N+1} E_{N->N+1}), F_d = l_d E_d with
+//   E_d = R_{N-d+1} E_{d-1}, carried as F_d = -1/(d+1) [(i+1) F_{d-1}(i+1,j) +
+//   (j+1) F_{d-1}(i,j+1) + (N-d+1-i-j) F_{d-1}(i,j)] (l_d / l_{d-1} = -(N-d+1)/(d+1))
+// in place in ascending order on the thread's shared-memory row E (degree-N layout), each F_d
+// written to the face's stack g in volume order through the stack table fst (face f's
+// entries: layer d, then j, then i, i + j <= N - d). Per point the same arithmetic as
+// lift_face_accumulate, so both lifts give the same stacks.
 template <class T>
 __device__ void chain_lift_runtime(int N, const T* __restrict__ x, T* __restrict__ E,
-                                   T* __restrict__ g, const uint16_t* __restrict__ fst,
-                                   const T* __restrict__ lj) {
+                                   T* __restrict__ g, const uint16_t* __restrict__ fst) {
   int rb = 0;  // row offset of row j in the degree-N triangle
   for (int j = 0; j <= N; ++j) {
     const int rlen = N + 1 - j;
@@ -131,16 +142,15 @@ __device__ void chain_lift_runtime(int N, const T* __restrict__ x, T* __restrict
   int s = rb;  // == np2(N): first entry of layer 1
   for (int d = 1; d <= N; ++d) {
     const int n = N - d + 1;  // input degree of this reduction
-    const T inv = T(1) / T(n);
-    const T w = lj[d];
+    const T cd = -inv_int<T>(d + 1);  // l_d / (l_{d-1} n)
     int r = 0;
     for (int j = 0; j < n; ++j) {
       const int rn = r + (N + 1 - j);  // next row in the degree-N layout
       for (int i = 0; i + j < n; ++i) {
         // in place, ascending: (i+1, j) and (i, j+1) are still degree-n values
-        const T v = reduce_point<T>(i, j, n, E[r + i + 1], E[rn + i], E[r + i], inv);
+        const T v = reduce_point<T>(i, j, n, E[r + i + 1], E[rn + i], E[r + i], cd);
         E[r + i] = v;
-        g[fst[s++]] = mul_rn(w, v);
+        g[fst[s++]] = v;
       }
       r = rn;
     }
@@ -153,11 +163,11 @@ TileLayout tile_layout(const DegTables& t, int epb) {
 }
 
 // One tile of the generic stage (all threads of the block call it). The degree tables are in
-// shared memory (st), sLj holds l_j(N); the layout L matches P's degree, physics and tile.
+// shared memory (st); the layout L matches P's degree, physics and tile.
 template <class T, int PHYS, bool CHAIN_LIFT = true>
 __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
                                    const SmemTables& st, int64_t tile) {
-  constexpr int NF = Phys<PHYS>::NF, NW = Phys<PHYS>::NW;
+  constexpr int NF = Phys<PHYS>::NF, NW = Phys<PHYS>::NW, NCH = Phys<PHYS>::NCH;
   extern __shared__ __align__(16) unsigned char smem[];
   T* sbase = reinterpret_cast<T*>(smem);
   T* sQ = sbase + L.q;
@@ -165,7 +175,6 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
   T* sFlux = sbase + L.flux;
   T* sWork = sbase + L.work;
   T* sGeo = sbase + L.geo;
-  T* sLj = sbase + L.lj;
   int32_t* sConn = reinterpret_cast<int32_t*>(smem + L.conn_bytes);
   const int N = P.tab.N, Np = P.tab.Np, NpM1 = P.tab.NpM1, Nfp = P.tab.Nfp;
   const int64_t K = P.K;
@@ -231,13 +240,13 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
         fl[0] = -(T(0.5) * d[0] * nx - T(0.5) * d[0] * Jf);
       } else if constexpr (PHYS == BB_WAVE) {
         // 3d_wave.jl:45-54
+        // the velocity flux 0.5 B (nx, ny, nz) is stored as the scalar 0.5 B; the lift
+        // multiplies its result by the normal
         const T ndotdU = nx * d[1] + ny * d[2] + nz * d[3];
         const T A = cp * d[0] - ndotdU;
         const T B = cu * ndotdU - d[0];
         fl[0] = T(0.5) * A;
-        fl[1] = T(0.5) * (B * nx);
-        fl[2] = T(0.5) * (B * ny);
-        fl[3] = T(0.5) * (B * nz);
+        fl[1] = T(0.5) * B;
       } else {
         // 3d_maxwell.jl:189-207: 0.5 (fx nx + fy ny + fz nz)(du) + 0.5 du - 0.5 n (n.d)
         const T Hx = d[0], Hy = d[1], Hz = d[2], Ex = d[3], Ey = d[4], Ez = d[5];
@@ -254,7 +263,7 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
       }
       T* fo = sFlux + ((size_t)(le * 4 + f) * NF) * Nfp + a;
 #pragma unroll
-      for (int fld = 0; fld < NF; ++fld) fo[(size_t)fld * Nfp] = fl[fld];
+      for (int ch = 0; ch < NCH; ++ch) fo[(size_t)ch * Nfp] = fl[ch];
     }
 
     // ---- 3a. volume term at degree N-1 -------------------------------------------------
@@ -324,22 +333,22 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
       if (i > 0) {
         const int x = ijk3(N - 1, i - 1, j, k);
 #pragma unroll
-        for (int m = 0; m < NW; ++m) acc[m] += T(i) * wb[m * ws + x];
+        for (int m = 0; m < NW; ++m) acc[m] += small_int<T>(i) * wb[m * ws + x];
       }
       if (j > 0) {
         const int x = ijk3(N - 1, i, j - 1, k);
 #pragma unroll
-        for (int m = 0; m < NW; ++m) acc[m] += T(j) * wb[m * ws + x];
+        for (int m = 0; m < NW; ++m) acc[m] += small_int<T>(j) * wb[m * ws + x];
       }
       if (k > 0) {
         const int x = ijk3(N - 1, i, j, k - 1);
 #pragma unroll
-        for (int m = 0; m < NW; ++m) acc[m] += T(k) * wb[m * ws + x];
+        for (int m = 0; m < NW; ++m) acc[m] += small_int<T>(k) * wb[m * ws + x];
       }
       if (l > 0) {
         const int x = ijk3(N - 1, i, j, k);
 #pragma unroll
-        for (int m = 0; m < NW; ++m) acc[m] += T(l) * wb[m * ws + x];
+        for (int m = 0; m < NW; ++m) acc[m] += small_int<T>(l) * wb[m * ws + x];
       }
 #pragma unroll
       for (int m = 0; m < NF; ++m)
@@ -349,39 +358,50 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
 
     // ---- 4. lift of the face fluxes, face t=-1 first as src/BernsteinLift.jl:202-205 ----
     if (CHAIN_LIFT && L.chain) {
-      // one thread per (element, face, field) chain; stacks land in volume order
-      const int nchain = ne * 4 * NF;
+      // one thread per (element, face, chain); stacks land in volume order
+      const int nchain = ne * 4 * NCH;
       const int rs = Nfp | 1;
-      T* sStack = sWork;                                // [epb*4*NF][Np]
-      T* sRow = sWork + (size_t)epb * 4 * NF * Np;      // [epb*4*NF][rs]
+      T* sStack = sWork;                                // [epb*4*NCH][Np]
+      T* sRow = sWork + (size_t)epb * 4 * NCH * Np;     // [epb*4*NCH][rs]
       for (int c = threadIdx.x; c < nchain; c += blockDim.x) {
-        const int f = (c / NF) & 3;                     // c = (le*4 + f)*NF + fld
-        chain_lift_runtime<T>(N, sFlux + (size_t)c * Nfp, sRow + (size_t)c * rs,
-                              sStack + (size_t)c * Np, st.fstack + (size_t)f * Np, sLj);
+        const int ef = c / NCH, ch = c - ef * NCH;      // c = (le*4 + f)*NCH + ch
+        chain_lift_runtime<T>(N, sFlux + ((size_t)ef * NF + ch) * Nfp, sRow + (size_t)c * rs,
+                              sStack + (size_t)c * Np, st.fstack + (size_t)(ef & 3) * Np);
       }
       __syncthreads();
+      // faces in the order 3, 0, 1, 2 (as lift_face_accumulate, so that both lifts agree)
       for (int it = threadIdx.x; it < ne * NF * Np; it += blockDim.x) {
         const int le = by_nfnp.div(it), rem = it - le * NF * Np;
         const int fld = by_np.div(rem), n = rem - fld * Np;
-        const T* g = sStack + ((size_t)le * 4 * NF + fld) * Np + n;  // face f at + f*NF*Np
         T* o = sOut + ((size_t)fld * epb + le) * Np + n;
         T acc = *o;
-        acc += g[(size_t)3 * NF * Np];
-        acc += g[0];
-        acc += g[(size_t)1 * NF * Np];
-        acc += g[(size_t)2 * NF * Np];
+        if (PHYS == BB_WAVE && fld > 0) {
+          // velocity component fld - 1: the scalar chain times that normal component
+          const T* g = sStack + ((size_t)le * 4 * NCH + 1) * Np + n;  // face f at + f*NCH*Np
+          const T* nc = sGeo + le * BB_GEO_STRIDE + 12 + 4 * (fld - 1);
+          acc = fma(nc[3], g[(size_t)3 * NCH * Np], acc);
+          acc = fma(nc[0], g[0], acc);
+          acc = fma(nc[1], g[(size_t)1 * NCH * Np], acc);
+          acc = fma(nc[2], g[(size_t)2 * NCH * Np], acc);
+        } else {
+          const T* g = sStack + ((size_t)le * 4 * NCH + fld) * Np + n;
+          acc += g[(size_t)3 * NCH * Np];
+          acc += g[0];
+          acc += g[(size_t)1 * NCH * Np];
+          acc += g[(size_t)2 * NCH * Np];
+        }
         *o = acc;
       }
       __syncthreads();
     } else {
-      const int order[4] = {3, 0, 1, 2};
       const int S = np2(N + 1);
       T* bufA = sWork;
-      T* bufB = sWork + (size_t)epb * NF * S;
+      T* bufB = sWork + (size_t)epb * NCH * S;
       for (int q = 0; q < 4; ++q) {
-        const int f = order[q];
-        lift_face_accumulate<T>(N, f, ne, NF, st.node2, sFlux + (size_t)f * NF * Nfp,
-                                4 * NF * Nfp, Nfp, sOut, Np, epb * Np, bufA, bufB, sLj);
+        const int f = (q + 3) & 3;  // faces 3, 0, 1, 2
+        lift_face_accumulate<T, PHYS == BB_WAVE>(N, f, ne, NCH, st.node2,
+                                                 sFlux + (size_t)f * NF * Nfp, 4 * NF * Nfp, Nfp,
+                                                 sOut, Np, epb * Np, bufA, bufB, sGeo + 12 + f);
       }
     }
 
