@@ -258,12 +258,14 @@ def main():
     ap.add_argument("--state-gb", type=float, default=2.0,
                     help="config 2: bytes of operator input state per operator, in GB")
     ap.add_argument("--dtypes", type=str, default="f32,f64", help="config 2: f32, f64 or both")
+    ap.add_argument("--mesh-n", type=int, default=32,
+                    help="config 3: hexes per side (32: the K = 196,608 workload; smaller for profiling)")
     a = ap.parse_args()
     if a.config == 2:
         lo, hi = (int(v) for v in a.degrees.split("-"))
         config2(range(lo, hi + 1), dtypes=tuple(a.dtypes.split(",")), state_bytes=a.state_gb * 1e9)
     elif a.config == 3:
-        config3(steps=a.steps or 200)
+        config3(steps=a.steps or 200, n=a.mesh_n)
     elif a.config == 4:
         config4(steps=a.steps or 100)
     else:
