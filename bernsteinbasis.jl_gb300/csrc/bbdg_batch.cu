@@ -137,7 +137,8 @@ int batch_tile_default(int N, int nf, int dtype) {
   // largest of 6, 4, 2, 1 elements whose generic tile fits in 100 KB of shared memory
   const int cands[4] = {6, 4, 2, 1};
   for (int e : cands) {
-    const TileLayout L = tile_layout_for(N, nf, nf, dtype_size(dtype), 1 << 12, e, kBatchChainLiftBytes);
+    const TileLayout L =
+        tile_layout_for(N, nf, nf, dtype_size(dtype), deg_table_words(N), e, kBatchChainLiftBytes);
     if (L.total <= 100 * 1024) return e;
   }
   return 1;
@@ -440,8 +441,9 @@ extern "C" int bb_batch_set_tile(bb_batch* b, int physics, int N, int elems_per_
   if (elems_per_block < 1 || elems_per_block > 64)
     return bb_fail(b->ctx, BB_ERR_ARG, "elements per block must be 1..64");
   const int nf = physics_nf(physics);
-  const TileLayout L = tile_layout_for(N, nf, nf, dtype_size(b->dtype), 1 << 12, elems_per_block,
-                                         kBatchChainLiftBytes);
+  if (!valid_degree(N) || nf == 0) return bb_fail(b->ctx, BB_ERR_ARG, "bad physics or degree");
+  const TileLayout L = tile_layout_for(N, nf, nf, dtype_size(b->dtype), deg_table_words(N),
+                                       elems_per_block, kBatchChainLiftBytes);
   if (L.total > b->ctx->smem_optin)
     return bb_fail(b->ctx, BB_ERR_ARG, "tile of %d elements exceeds shared memory", elems_per_block);
   int hits = 0;

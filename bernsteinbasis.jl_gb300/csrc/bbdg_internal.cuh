@@ -75,6 +75,12 @@ struct DegTables {
   int nwords = 0;
   uint32_t* d_words = nullptr;
 };
+// 32-bit words of the degree-N tables, the sum of the DegTables sections above in order
+// (shared-memory sizes of a tile are computed from it before the tables exist).
+inline int deg_table_words(int N) {
+  return np3(N) + np3(N - 1) + (np3(N + 1) + 1) / 2 + (4 * np2(N) + 1) / 2 +
+         (6 * np2(N) + 1) / 2 + (4 * np3(N) + 1) / 2 + (np3(N) + 1) / 2;
+}
 
 // Orientation codes: face vertex m of this side is face vertex PERMS[o][m] of the partner,
 // PERMS = (0,1,2),(0,2,1),(1,0,2),(1,2,0),(2,0,1),(2,1,0), packed 2 bits per entry.

@@ -113,6 +113,10 @@ const DegTables* bb_tables(bb_ctx* ctx, int N) {
   t->o_fstack = off; off += (4 * t->Np + 1) / 2;
   t->o_sslot = off; off += (t->Np + 1) / 2;
   t->nwords = off;
+  if (off != deg_table_words(N)) {  // the tile-size estimates rely on the same count
+    delete t;
+    return nullptr;
+  }
   std::vector<uint32_t> w(off, 0u);
   auto put16 = [&](int word_off, int idx, int v) {
     uint16_t* p = reinterpret_cast<uint16_t*>(w.data() + word_off);

@@ -402,9 +402,7 @@ extern "C" int bb_stage_tile_bytes(int physics, int N, int dtype, int epb, int64
   if (physics_nf(physics) == 0 || !valid_degree(N) || !valid_dtype(dtype) || epb < 1 ||
       epb > 64 || !bytes)
     return BB_ERR_ARG;
-  // table words of degree N: node3, node3m1, node2 (u16), fvol, fperm, fstack (u16)
-  const int nwords = np3(N) + np3(N - 1) + (np3(N + 1) + 1) / 2 + (4 * np2(N) + 1) / 2 +
-                     (6 * np2(N) + 1) / 2 + (4 * np3(N) + 1) / 2;
+  const int nwords = deg_table_words(N);
   const int nf = physics_nf(physics);
   const TileLayout L = tile_layout_for(N, nf, nf, dtype_size(dtype), nwords, epb);
   *bytes = (int64_t)L.total;

@@ -63,10 +63,10 @@ struct StageParams {
 };
 
 // Shared-memory layout of a tile (in units of T unless noted). chain != 0: the lift runs one
-// thread per (element, face, field) chain with the face stacks in shared memory (used when
-// that fits in kChainLiftBytes); chain == 0: the level-parallel lift with two ping-pong rows.
+// thread per (element, face, chain) with the face stacks in shared memory (FP32 tiles that fit
+// in kChainLiftBytes); chain == 0: the level-parallel lift with two ping-pong rows.
 struct TileLayout {
-  size_t q, out, flux, work, geo, conn_bytes, tab_bytes, total;
+  size_t q, out, flux, work, geo, pen, conn_bytes, tab_bytes, total;
   int work_elems;
   int chain;
 };
@@ -97,6 +97,7 @@ __host__ __device__ inline TileLayout tile_layout_with(int N, int NF, int NW, si
   L.work_elems = (int)(wvol > wlift ? wvol : wlift);
   off += L.work_elems;
   L.geo = off; off += (size_t)epb * BB_GEO_STRIDE;
+  L.pen = off; off += (size_t)epb * 8;  // per face: tau |n|, tau / |n|
   size_t bytes = align16(off * tsize);
   L.conn_bytes = bytes; bytes += align16((size_t)epb * 4 * sizeof(int32_t));
   L.tab_bytes = bytes; bytes += (size_t)nwords * 4;
@@ -175,6 +176,7 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
   T* sFlux = sbase + L.flux;
   T* sWork = sbase + L.work;
   T* sGeo = sbase + L.geo;
+  T* sPen = sbase + L.pen;
   int32_t* sConn = reinterpret_cast<int32_t*>(smem + L.conn_bytes);
   const int N = P.tab.N, Np = P.tab.Np, NpM1 = P.tab.NpM1, Nfp = P.tab.Nfp;
   const int64_t K = P.K;
@@ -188,7 +190,21 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
     for (int fld = 0; fld < NF; ++fld)
       copy_g2s(sQ + (size_t)fld * epb * Np, P.q + ((size_t)fld * K + e0) * Np, ne * Np);
     copy_g2s(sGeo, P.geo + e0 * BB_GEO_STRIDE, ne * BB_GEO_STRIDE);
-    for (int t = threadIdx.x; t < ne * 4; t += blockDim.x) sConn[t] = __ldg(P.conn + e0 * 4 + t);
+    for (int t = threadIdx.x; t < ne * 4; t += blockDim.x) {
+      sConn[t] = __ldg(P.conn + e0 * 4 + t);
+      // the face's penalty weights (tau |n|, tau / |n|; 1 and 1 with tau <= 0), once per face:
+      // a square root and a division are long sequences on the FP64 pipe
+      const T* g = P.geo + (e0 + (t >> 2)) * BB_GEO_STRIDE + 12 + (t & 3);
+      const T nx = __ldg(g), ny = __ldg(g + 4), nz = __ldg(g + 8);
+      T cp = T(1), cu = T(1);
+      if (P.tau > T(0)) {
+        const T Jf = sqrt(nx * nx + ny * ny + nz * nz);
+        cp = P.tau * Jf;
+        cu = P.tau / Jf;
+      }
+      sPen[2 * t] = cp;
+      sPen[2 * t + 1] = cu;
+    }
     __syncthreads();
 
     // ---- 2. interface flux -------------------------------------------------------------
@@ -227,12 +243,7 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
       }
       const T* g = sGeo + le * BB_GEO_STRIDE;
       const T nx = g[12 + f], ny = g[16 + f], nz = g[20 + f];
-      T cp = T(1), cu = T(1);
-      if (P.tau > T(0)) {
-        const T Jf = sqrt(nx * nx + ny * ny + nz * nz);
-        cp = P.tau * Jf;
-        cu = P.tau / Jf;
-      }
+      const T cp = sPen[(le * 4 + f) * 2], cu = sPen[(le * 4 + f) * 2 + 1];
       T fl[NF];
       if constexpr (PHYS == BB_ADVECTION) {
         // 3d_advec_scalar.jl:24-29: 0.5 du nxJ - 0.5 du Jf (negated, see Phys<BB_ADVECTION>)

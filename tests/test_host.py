@@ -29,6 +29,41 @@ def test_capi_library_exports_every_declared_symbol():
     assert set(names) <= set(_lib.SIGNATURES), set(names) - set(_lib.SIGNATURES)
 
 
+def test_generic_tile_lift_form_and_size():
+    """bb_stage_tile_bytes (host arithmetic only): FP64 tiles always lift level by level, an
+    FP32 tile takes the chain-per-thread lift exactly when that tile fits in 100 KB, and every
+    size counts the degree tables in full (the stack-slot table included)."""
+    from bbdg import _lib
+    lib = _lib.load()
+    b, c = ctypes.c_int64(), ctypes.c_int()
+
+    def tile(phys, N, dtype, epb):
+        assert lib.bb_stage_tile_bytes(phys, N, dtype, epb, ctypes.byref(b), ctypes.byref(c)) == 0
+        return b.value, c.value
+
+    def np3(n):
+        return (n + 1) * (n + 2) * (n + 3) // 6
+
+    def np2(n):
+        return (n + 1) * (n + 2) // 2
+
+    for phys in (0, 1, 2):
+        for N in (1, 3, 9, 15, 20):
+            words = (np3(N) + np3(N - 1) + (np3(N + 1) + 1) // 2 + (4 * np2(N) + 1) // 2
+                     + (6 * np2(N) + 1) // 2 + (4 * np3(N) + 1) // 2 + (np3(N) + 1) // 2)
+            for epb in (1, 2, 4, 8):
+                b64, c64 = tile(phys, N, 1, epb)
+                assert c64 == 0 and b64 >= 4 * words
+                b32, c32 = tile(phys, N, 0, epb)
+                assert b32 >= 4 * words
+                if c32:
+                    assert b32 <= 100 * 1024
+    # the benchmark's degree: an FP32 2-element wave tile lifts chain per thread (two chains
+    # per face), the FP64 one level by level
+    assert tile(0, 9, 0, 2)[1] == 1 and tile(0, 9, 1, 2)[1] == 0
+    assert lib.bb_stage_tile_bytes(0, 0, 0, 2, ctypes.byref(b), ctypes.byref(c)) != 0
+
+
 def neighbour_node(N, o, a_idx):
     """Face node a of this side -> node index on the partner side (orientation o)."""
     from bbdg.mesh import PERMS
