@@ -66,7 +66,7 @@ struct StageParams {
 // thread per (element, face, chain) with the face stacks in shared memory (FP32 tiles that fit
 // in kChainLiftBytes); chain == 0: the level-parallel lift with two ping-pong rows.
 struct TileLayout {
-  size_t q, out, flux, work, geo, pen, conn_bytes, tab_bytes, total;
+  size_t q, out, flux, work, geo, pen, gh, conn_bytes, tab_bytes, total;
   int work_elems;
   int chain;
 };
@@ -98,6 +98,7 @@ __host__ __device__ inline TileLayout tile_layout_with(int N, int NF, int NW, si
   off += L.work_elems;
   L.geo = off; off += (size_t)epb * BB_GEO_STRIDE;
   L.pen = off; off += (size_t)epb * 8;  // per face: tau |n|, tau / |n|
+  L.gh = off; off += (size_t)epb * 9;   // per element: rxJ ... txJ / 2
   size_t bytes = align16(off * tsize);
   L.conn_bytes = bytes; bytes += align16((size_t)epb * 4 * sizeof(int32_t));
   L.tab_bytes = bytes; bytes += (size_t)nwords * 4;
@@ -177,6 +178,7 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
   T* sWork = sbase + L.work;
   T* sGeo = sbase + L.geo;
   T* sPen = sbase + L.pen;
+  T* sGh = sbase + L.gh;
   int32_t* sConn = reinterpret_cast<int32_t*>(smem + L.conn_bytes);
   const int N = P.tab.N, Np = P.tab.Np, NpM1 = P.tab.NpM1, Nfp = P.tab.Nfp;
   const int64_t K = P.K;
@@ -204,6 +206,12 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
       }
       sPen[2 * t] = cp;
       sPen[2 * t + 1] = cu;
+    }
+    // barycentric weights of J d/dx, J d/dy, J d/dz: g_a = (rxJ, sxJ, txJ, -sum) / 2, once
+    // per element rather than per volume point
+    for (int t = threadIdx.x; t < ne * 9; t += blockDim.x) {
+      const int le = t / 9;
+      sGh[t] = T(0.5) * __ldg(P.geo + (e0 + le) * BB_GEO_STRIDE + (t - le * 9));
     }
     __syncthreads();
 
@@ -284,13 +292,11 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
       const int i = c & 0xff, j = (c >> 8) & 0xff, k = c >> 16;
       const int idx[4] = {ijk3(N, i + 1, j, k), ijk3(N, i, j + 1, k), ijk3(N, i, j, k + 1),
                           ijk3(N, i, j, k)};
-      const T* g = sGeo + le * BB_GEO_STRIDE;
-      // barycentric weights of d/dx, d/dy, d/dz (times J): g_a = (rxJ, sxJ, txJ, -sum)/2;
-      // the fourth weight is implied by the differences below
-      T gx[3], gy[3], gz[3];
-      gx[0] = T(0.5) * g[0]; gx[1] = T(0.5) * g[1]; gx[2] = T(0.5) * g[2];
-      gy[0] = T(0.5) * g[3]; gy[1] = T(0.5) * g[4]; gy[2] = T(0.5) * g[5];
-      gz[0] = T(0.5) * g[6]; gz[1] = T(0.5) * g[7]; gz[2] = T(0.5) * g[8];
+      // barycentric weights of d/dx, d/dy, d/dz (times J), staged per element; the fourth
+      // weight is implied by the differences below
+      const T* gx = sGh + le * 9;  // gx[a], then gy = gx + 3, gz = gx + 6
+      const T* gy = gx + 3;
+      const T* gz = gx + 6;
       const T* q0 = sQ + (size_t)le * Np;
       auto F = [&](int fld, int a) { return q0[(size_t)fld * epb * Np + idx[a]]; };
       T w[NW];
@@ -363,7 +369,7 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
       }
 #pragma unroll
       for (int m = 0; m < NF; ++m)
-        sOut[((size_t)m * epb + le) * Np + n] = T(Phys<PHYS>::vol_sign) * acc[m];
+        sOut[((size_t)m * epb + le) * Np + n] = Phys<PHYS>::vol_sign < 0 ? -acc[m] : acc[m];
     }
     __syncthreads();
 
