@@ -268,6 +268,21 @@ __device__ __forceinline__ double half_int_f64(int v) {
   return __hiloint2double(v ? (int)hi : 0, 0);
 }
 
+// Weights of a sum that is halved at the end (the derivative rows): in double the weight is
+// v / 2 and the final product by 1/2 is dropped (finish_half returns the sum); every partial
+// sum is then exactly half of the unhalved one, so the bits are the same and the FP64 pipe
+// does one product less per output. In float the weight is v and the sum is halved.
+template <class T>
+__device__ __forceinline__ T halved_weight(int v) {
+  if constexpr (sizeof(T) == 8) return half_int_f64(v);
+  else return small_int<T>(v);
+}
+template <class T>
+__device__ __forceinline__ T finish_half(T v) {
+  if constexpr (sizeof(T) == 8) return v;
+  else return T(0.5) * v;
+}
+
 // L0 x at face node (i, j) of degree N, k = N - i - j: the 7-point stencil of
 // (N+1)^2/2 R_{N+1} E_{N->N+1} (src/BernsteinLift.jl:100-125 then :66-90 with the L0
 // scaling), x in the 2D layout of degree N with row offsets rb (row j), rbn (row j+1) and

@@ -176,7 +176,8 @@ const DegTables* bb_tables(bb_ctx* ctx, int N) {
 // derivative kernels
 // -------------------------------------------------------------------------------------
 // (D x)_row for one axis, written as the reference does (fast_D{r,s,t}_multiply!):
-// val = sum of (multi-index entry) * (difference of two neighbours), out = val / 2.
+// val = sum of (multi-index entry) * (difference of two neighbours), out = val / 2 (in
+// double the halving rides in the weights, halved_weight / finish_half).
 template <class T>
 __device__ __forceinline__ T deriv_row(int axis, int N, const T* x, int i, int j, int k, int row) {
   const int l = N - i - j - k;
@@ -184,29 +185,29 @@ __device__ __forceinline__ T deriv_row(int axis, int N, const T* x, int i, int j
   T val;
   if (axis == 0) {  // BernsteinDerivativeMatrix_3D.jl:96-132
     T x4 = (i > 0) ? x[ijk3(N, i - 1, j, k)] : T(0);
-    val = small_int<T>(i) * (xr - x4);
-    if (j > 0) val += small_int<T>(j) * (x[ijk3(N, i + 1, j - 1, k)] - x[ijk3(N, i, j - 1, k)]);
-    if (k > 0) val += small_int<T>(k) * (x[ijk3(N, i + 1, j, k - 1)] - x[ijk3(N, i, j, k - 1)]);
+    val = halved_weight<T>(i) * (xr - x4);
+    if (j > 0) val += halved_weight<T>(j) * (x[ijk3(N, i + 1, j - 1, k)] - x[ijk3(N, i, j - 1, k)]);
+    if (k > 0) val += halved_weight<T>(k) * (x[ijk3(N, i + 1, j, k - 1)] - x[ijk3(N, i, j, k - 1)]);
     T x1 = (l > 0) ? x[ijk3(N, i + 1, j, k)] : T(0);
-    val += small_int<T>(l) * (x1 - xr);
+    val += halved_weight<T>(l) * (x1 - xr);
   } else if (axis == 1) {  // :138-174
     val = T(0);
-    if (i > 0) val = small_int<T>(i) * (x[ijk3(N, i - 1, j + 1, k)] - x[ijk3(N, i - 1, j, k)]);
+    if (i > 0) val = halved_weight<T>(i) * (x[ijk3(N, i - 1, j + 1, k)] - x[ijk3(N, i - 1, j, k)]);
     T x4 = (j > 0) ? x[ijk3(N, i, j - 1, k)] : T(0);
-    val += small_int<T>(j) * (xr - x4);
-    if (k > 0) val += small_int<T>(k) * (x[ijk3(N, i, j + 1, k - 1)] - x[ijk3(N, i, j, k - 1)]);
+    val += halved_weight<T>(j) * (xr - x4);
+    if (k > 0) val += halved_weight<T>(k) * (x[ijk3(N, i, j + 1, k - 1)] - x[ijk3(N, i, j, k - 1)]);
     T x2 = (l > 0) ? x[ijk3(N, i, j + 1, k)] : T(0);
-    val += small_int<T>(l) * (x2 - xr);
+    val += halved_weight<T>(l) * (x2 - xr);
   } else {  // :180-216
     val = T(0);
-    if (i > 0) val = small_int<T>(i) * (x[ijk3(N, i - 1, j, k + 1)] - x[ijk3(N, i - 1, j, k)]);
-    if (j > 0) val += small_int<T>(j) * (x[ijk3(N, i, j - 1, k + 1)] - x[ijk3(N, i, j - 1, k)]);
+    if (i > 0) val = halved_weight<T>(i) * (x[ijk3(N, i - 1, j, k + 1)] - x[ijk3(N, i - 1, j, k)]);
+    if (j > 0) val += halved_weight<T>(j) * (x[ijk3(N, i, j - 1, k + 1)] - x[ijk3(N, i, j - 1, k)]);
     T x4 = (k > 0) ? x[ijk3(N, i, j, k - 1)] : T(0);
-    val += small_int<T>(k) * (xr - x4);
+    val += halved_weight<T>(k) * (xr - x4);
     T x3 = (l > 0) ? x[ijk3(N, i, j, k + 1)] : T(0);
-    val += small_int<T>(l) * (x3 - xr);
+    val += halved_weight<T>(l) * (x3 - xr);
   }
-  return T(0.5) * val;
+  return finish_half(val);
 }
 
 // Applies up to three derivative operators (mask bits r,s,t) to EPB element columns per
@@ -303,13 +304,13 @@ __global__ void __launch_bounds__(256) deriv_fact_kernel(DegTables tab,
       const uint2 ga = sGA[n];
       const uint32_t gw = sGW[n];
       const int m0 = ga.x & 0xffff, m1 = ga.x >> 16, m2 = ga.y & 0xffff, m3 = ga.y >> 16;
-      const T a0 = small_int<T>(gw & 0xff), a1 = small_int<T>((gw >> 8) & 0xff),
-              a2 = small_int<T>((gw >> 16) & 0xff), a3 = small_int<T>(gw >> 24);
+      const T a0 = halved_weight<T>(gw & 0xff), a1 = halved_weight<T>((gw >> 8) & 0xff),
+              a2 = halved_weight<T>((gw >> 16) & 0xff), a3 = halved_weight<T>(gw >> 24);
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
         if (!(mask & (1 << a))) continue;
         const T* w = sW + ((size_t)a * epb + le) * NW;
-        outs[a][e0 * Np + it] = T(0.5) * (a0 * w[m0] + a1 * w[m1] + a2 * w[m2] + a3 * w[m3]);
+        outs[a][e0 * Np + it] = finish_half(a0 * w[m0] + a1 * w[m1] + a2 * w[m2] + a3 * w[m3]);
       }
     }
   }
