@@ -26,9 +26,15 @@
 
 namespace {
 
+// The reference's offset tuples hold 21 entries (ordering.jl:8-26): enough for degree 20,
+// not for the degree N + 1 = 21 that the lift of degree 20 elevates to (row 21 of that
+// triangle), so the reference's lift stops at N = 19. These tables run two entries further by
+// the same formula, so that the library's N = 20 lift is checked; oracle_offsets exports the
+// reference's 21.
+constexpr int kOffsets = 23;
 struct Offsets {
-  int tri[21];
-  int tet[21];
+  int tri[kOffsets];
+  int tet[kOffsets];
 };
 
 // ordering.jl:8-26 (tri_offsets / tet_offsets)
@@ -37,7 +43,7 @@ Offsets make_offsets(int N) {
   o.tri[0] = 0;
   o.tet[0] = 0;
   int c2 = 0, c3 = 0;
-  for (int i = 1; i <= 20; ++i) {
+  for (int i = 1; i < kOffsets; ++i) {
     c2 += N + 2 - i;
     c3 += ((N + 2 - i) * (N + 3 - i)) / 2;
     o.tri[i] = c2;

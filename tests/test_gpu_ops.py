@@ -47,10 +47,11 @@ def test_derivative_matches_oracle(cuda, bb, oracle_cpu, N, dt):
 
 @pytest.mark.parametrize("K", [29, 1000])
 @pytest.mark.parametrize("dt", ["f64", "f32"])
-@pytest.mark.parametrize("N", range(1, 16))
+@pytest.mark.parametrize("N", range(1, 21))
 def test_lift_matches_oracle(cuda, bb, oracle_cpu, N, dt, K):
-    """FP32 degrees 1..15 run the degree-specialised register-chain kernels, FP64 the
-    level-parallel one; K = 29 leaves a ragged last tile, K = 1000 spans many tiles."""
+    """FP32 degrees 1..15 run the degree-specialised register-chain kernels, FP64 and FP32
+    16..20 the level-parallel one; K = 29 leaves a ragged last tile, K = 1000 spans many
+    tiles."""
     import torch
     rng = np.random.default_rng(50 + N)
     Np, Nfp = bb.np3(N), bb.np2(N)
