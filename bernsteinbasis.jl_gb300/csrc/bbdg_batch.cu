@@ -177,9 +177,8 @@ int build_desc(bb_batch* b) {
     if (b->fast[p] >= 0) continue;
     const bb_batch_problem& pr = b->probs[p];
     const DegTables* t = b->tabs[p];
-    h.emplace_back();
+    h.push_back(BatchDesc<T>{});  // every field zero (the degree tables' own defaults)
     BatchDesc<T>& d = h.back();
-    memset(&d, 0, sizeof(d));
     d.P.tab = *t;
     d.P.gtab = t->d_words;
     d.P.K = pr.K;
