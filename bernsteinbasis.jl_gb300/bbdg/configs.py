@@ -23,7 +23,7 @@ import numpy as np
 import torch
 
 from . import autotune
-from .batch import BatchSolver, config4_problems, NFIELDS
+from .batch import BatchSolver, config4_problems
 from .mesh import uniform_tet_mesh
 from .operators import (BernsteinDerivativeMatrix_3D_r, BernsteinDerivativeMatrix_3D_s,
                         BernsteinDerivativeMatrix_3D_t, BernsteinLift, fused_apply_, grad_,

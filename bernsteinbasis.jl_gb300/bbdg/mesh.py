@@ -22,7 +22,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .ordering import np3, linear_to_ijkl_lookup
+from .ordering import linear_to_ijkl_lookup
 
 # Face-local vertices (A, B, C) of each reference face, as element-vertex numbers (0-based,
 # StartUpDG order). f1: j=0, f2: l=0, f3: i=0, f4: k=0.

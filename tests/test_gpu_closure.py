@@ -10,7 +10,6 @@ rollout, are measured by `python -m bbdg.configs --config 5`).
 """
 import math
 
-import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
