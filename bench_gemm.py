@@ -1,6 +1,6 @@
 """Measurement of the tcgen05 BF16 GEMM on the closure MLP's shapes and a large square shape.
 
-  python -m bbdg.gemmbench [--reps R] [--shapes M,N,K;M,N,K...] [--no-cublas]
+  python bench_gemm.py [--reps R] [--shapes M,N,K;M,N,K...] [--no-cublas]
 
 Prints one JSON line per shape: our kernel's time and TFLOP/s with an FP32 and with a BF16
 output, cuBLAS (torch.matmul, BF16 output) on the same operands for comparison, and the
@@ -15,9 +15,17 @@ import argparse
 import json
 import os
 
-import torch
+import sys
 
-from . import mlp
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "bernsteinbasis.jl_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import torch  # noqa: E402
+
+from bbdg import mlp  # noqa: E402
 
 CLOSURE_SHAPES = [(24576, 512, 840), (24576, 512, 512), (24576, 336, 512), (512, 840, 24576),
                   (512, 512, 24576), (336, 512, 24576)]
@@ -25,7 +33,7 @@ SQUARE_SHAPES = [(8192, 8192, 8192)]
 
 
 def _peak_tflops():
-    root = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    root = ROOT
     try:
         with open(os.path.join(root, "MEASURED_PEAKS.json")) as fh:
             return float(json.load(fh)["bf16_tflops"]), "measured"

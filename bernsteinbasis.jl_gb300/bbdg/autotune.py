@@ -46,9 +46,25 @@ CANDIDATES = {
 GENERIC = [("generic", e, 256) for e in (1, 2, 4, 6, 12)]
 
 
+_LIB_HASH = None
+
+
+def _lib_hash() -> str:
+    """Content hash of the loaded libbbdg.so: a rebuilt library invalidates cached choices."""
+    global _LIB_HASH
+    if _LIB_HASH is None:
+        import hashlib
+        h = hashlib.sha1()
+        with open(_build.LIB, "rb") as fh:
+            for chunk in iter(lambda: fh.read(1 << 20), b""):
+                h.update(chunk)
+        _LIB_HASH = h.hexdigest()[:16]
+    return _LIB_HASH
+
+
 def _key(solver) -> str:
     name = torch.cuda.get_device_name(solver.device)
-    return f"{solver.physics}|{solver.N}|{str(solver.dtype)}|K={solver.K}|{name}"
+    return f"{solver.physics}|{solver.N}|{str(solver.dtype)}|K={solver.K}|{name}|lib={_lib_hash()}"
 
 
 def _load():

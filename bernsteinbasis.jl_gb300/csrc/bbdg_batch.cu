@@ -480,7 +480,7 @@ extern "C" int bb_batch_run(bb_batch* b, int nsteps, int use_graph, void* stream
   BB_CUDA(b->ctx, cudaStreamSynchronize(st));
   if (h) {
     cudaMemsetAsync(b->d_status, 0, sizeof(int), st);
-    return bb_fail(b->ctx, BB_ERR_DEVICE, "device check failed (corrupt connectivity)");
+    return bb_device_status_error(b->ctx, h);
   }
   return BB_OK;
 }

@@ -132,6 +132,10 @@ int bb_lift_fast(bb_ctx* ctx, const DegTables* t, int64_t K, int nfaces, const v
 int bb_set_device(bb_ctx* ctx);
 // Checks a launch and counts it.
 int bb_check_launch(bb_ctx* ctx, const char* what);
+// Error for a nonzero device status word. Bit 0: a kernel found corrupt connectivity (a
+// neighbour index or orientation out of range) and skipped the access; bit 1: a bounded
+// device-side wait ran out and the kernel returned early. A time-out takes precedence.
+int bb_device_status_error(bb_ctx* ctx, int word);
 
 inline size_t dtype_size(int dtype) { return dtype == BB_F64 ? 8 : 4; }
 // Fields of a physics code, 0 if unknown.

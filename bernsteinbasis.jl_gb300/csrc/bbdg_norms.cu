@@ -274,21 +274,55 @@ static __device__ __align__(256) double g_noalloc_partials[kNoAllocBlocks * kMax
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
 double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+void* g_noalloc_ctx[kNoAllocMaxDevices] = {};  // driver context the address belongs to
 
-// Device address of g_noalloc_partials on the current device, looked up once per device.
-// (In host code the array's name is only a host-side stand-in, not a device address.)
+using CtxGetCurrentFn = int (*)(void**);  // cuCtxGetCurrent(CUcontext*)
+
+// The calling thread's current driver context, or nullptr if it cannot be read. A device's
+// primary context is replaced by cudaDeviceReset; the module, and with it the array, is then
+// loaded again, possibly at another address.
+void* current_driver_context() {
+  static CtxGetCurrentFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<CtxGetCurrentFn>(f);
+  }();
+  void* c = nullptr;
+  if (!fn || fn(&c) != 0) return nullptr;
+  return c;
+}
+
+// Device address of g_noalloc_partials on the current device, looked up once per device (and
+// again if the device's context was replaced). In host code the array's name is only a
+// host-side stand-in, not a device address.
 int noalloc_scratch(double** out) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices)
     return BB_ERR_CUDA;
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
+  void* c = current_driver_context();
+  if (!g_noalloc_ptr[dev] || c != g_noalloc_ctx[dev]) {
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_noalloc_partials) != cudaSuccess || !p) return BB_ERR_CUDA;
     g_noalloc_ptr[dev] = static_cast<double*>(p);
+    g_noalloc_ctx[dev] = c;
   }
   *out = g_noalloc_ptr[dev];
   return BB_OK;
+}
+
+// Launches through cudaLaunchKernel, whose return value belongs to this launch alone: an error
+// left pending by some earlier, unrelated runtime call is neither reported nor cleared here.
+// A launch error of our own is cleared so that it does not surface in a later caller's check.
+int noalloc_launch(const void* fn, int grid, void** args, cudaStream_t st) {
+  cudaError_t e = cudaLaunchKernel(fn, dim3(grid), dim3(kRedThreads), args, 0, st);
+  if (e == cudaSuccess) return BB_OK;
+  (void)cudaGetLastError();
+  return BB_ERR_CUDA;
 }
 
 }  // namespace
@@ -301,16 +335,14 @@ extern "C" int bb_norms_noalloc(int N, int64_t K, int nf, int dtype, const void*
   int rc = noalloc_scratch(&part);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
-  const int64_t n = K * np3(N);
+  int64_t n = K * np3(N);
   // every block writes all of its partials before sum_rows reads them: nothing to clear
-  if (dtype == BB_F64)
-    norms_partial<double><<<kNoAllocBlocks, kRedThreads, 0, st>>>(n, nf, (const double*)a,
-                                                                  (const double*)b, part);
-  else
-    norms_partial<float><<<kNoAllocBlocks, kRedThreads, 0, st>>>(n, nf, (const float*)a,
-                                                                 (const float*)b, part);
-  if (cudaGetLastError() != cudaSuccess) return BB_ERR_CUDA;
-  sum_rows<<<1, kRedThreads, 0, st>>>(kNoAllocBlocks, nf * 3, part, out_dev);
-  if (cudaGetLastError() != cudaSuccess) return BB_ERR_CUDA;
-  return BB_OK;
+  void* pargs[] = {&n, &nf, const_cast<void**>(&a), const_cast<void**>(&b), &part};
+  const void* partial = dtype == BB_F64 ? (const void*)norms_partial<double>
+                                        : (const void*)norms_partial<float>;
+  rc = noalloc_launch(partial, kNoAllocBlocks, pargs, st);
+  if (rc) return rc;
+  int nrows = kNoAllocBlocks, width = nf * 3;
+  void* sargs[] = {&nrows, &width, &part, &out_dev};
+  return noalloc_launch((const void*)sum_rows, 1, sargs, st);
 }

@@ -37,6 +37,13 @@ int bb_check_launch(bb_ctx* ctx, const char* what) {
   return BB_OK;
 }
 
+int bb_device_status_error(bb_ctx* ctx, int word) {
+  if (word & 2)
+    return bb_fail(ctx, BB_ERR_TIMEOUT, "a device-side bounded wait ran out (status 0x%x)", word);
+  return bb_fail(ctx, BB_ERR_DEVICE, "device check failed: corrupt connectivity (status 0x%x)",
+                 word);
+}
+
 extern "C" int bb_version(void) { return 10000; }
 
 extern "C" int bb_ctx_create(int device, bb_ctx** out) {

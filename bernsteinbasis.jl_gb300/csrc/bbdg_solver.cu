@@ -219,7 +219,7 @@ int check_status(bb_solver* s, cudaStream_t st) {
   BB_CUDA(s->ctx, cudaStreamSynchronize(st));
   if (h) {
     cudaMemsetAsync(s->d_status, 0, sizeof(int), st);
-    return bb_fail(s->ctx, BB_ERR_DEVICE, "device check failed (corrupt connectivity)");
+    return bb_device_status_error(s->ctx, h);
   }
   return BB_OK;
 }

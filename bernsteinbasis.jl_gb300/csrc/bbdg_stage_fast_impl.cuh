@@ -19,7 +19,7 @@
 // Wave (examples/3d_wave.jl:45-54): with affine elements the scaled normal n is constant on
 // a face, so the u, v, w fluxes are B n_x, B n_y, B n_z with B = (cu n.du - dp)/2: two chains
 // per face (A = (cp dp - n.du)/2 and B) instead of four.
-// Maxwell (examples/3d_maxwell.jl:189-207): six flux components, six chains per face.
+// Maxwell (examples/3d_maxwell.jl:43-65): six flux components, six chains per face.
 //
 // Block organisation: EPB elements per tile; TPE "element threads" per element plus
 // CHT "chain threads" (whole warps, one lift chain each). Tiles stream through a persistent

@@ -4,7 +4,7 @@
 // One thread block owns a tile of `epb` consecutive elements and does, per RK stage:
 //   1. stage q (all fields), geometry and connectivity of its tile in shared memory
 //   2. interface flux at every face node (examples/3d_wave.jl:41-56,
-//      examples/3d_maxwell.jl:185-209): the neighbour trace comes from shared memory when
+//      examples/3d_maxwell.jl:43-65): the neighbour trace comes from shared memory when
 //      the neighbour is in the same tile, otherwise from the trace buffer written by the
 //      previous stage (only faces that cross a tile boundary are ever written or read)
 //   3. volume term (3d_wave.jl:59-79): the geometric combination of Dr, Ds, Dt is applied
@@ -267,7 +267,7 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
         fl[0] = T(0.5) * A;
         fl[1] = T(0.5) * B;
       } else {
-        // 3d_maxwell.jl:189-207: 0.5 (fx nx + fy ny + fz nz)(du) + 0.5 du - 0.5 n (n.d)
+        // 3d_maxwell.jl:52-63: 0.5 (fx nx + fy ny + fz nz)(du) + 0.5 du - 0.5 n (n.d)
         const T Hx = d[0], Hy = d[1], Hz = d[2], Ex = d[3], Ey = d[4], Ez = d[5];
         const T ndH = nx * Hx + ny * Hy + nz * Hz;
         const T ndE = nx * Ex + ny * Ey + nz * Ez;

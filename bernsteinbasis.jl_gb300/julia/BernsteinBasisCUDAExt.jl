@@ -17,6 +17,7 @@ module BernsteinBasisCUDAExt
 using BernsteinBasis
 using CUDA
 using LinearAlgebra
+using StaticArrays
 
 const libbbdg = get(ENV, "BBDG_LIB", joinpath(@__DIR__, "..", "_build", "libbbdg.so"))
 

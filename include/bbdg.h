@@ -94,9 +94,10 @@ int bb_elevation_apply(bb_ctx* ctx, int N, int64_t K, int dtype, const void* x, 
 int bb_reduction_apply(bb_ctx* ctx, int N, int64_t K, int dtype, const void* x, void* out,
                        void* stream);
 
-/* Fused operator pass: dr, ds, dt = D{r,s,t} x and lift = L faces (one launch; in FP32 with
- * N <= 15 the gradient and lift kernels back to back, whose results equal bb_grad_apply and
- * bb_lift_apply bitwise). */
+/* Fused operator pass: dr, ds, dt = D{r,s,t} x and lift = L faces. In FP32 with N <= 15
+ * this is two launches, the gradient kernel and then the lift kernel, whose results equal
+ * bb_grad_apply and bb_lift_apply bitwise; otherwise (FP64, N > 15) one launch of the
+ * table-driven fused kernel. */
 int bb_fused_apply(bb_ctx* ctx, int N, int64_t K, int dtype, const void* x,
                    const void* faces, void* dr, void* ds, void* dt, void* lift, void* stream);
 
@@ -202,15 +203,17 @@ int bb_norms(bb_ctx* ctx, int N, int64_t K, int nf, int dtype, const void* a, co
              double* out_host, void* stream);
 
 /* The sums of bb_norms written to a caller-provided DEVICE buffer out_dev (3*nf doubles,
- * same order), without allocating anything and without a context: for callers that must not
- * allocate device memory -- code running while a CUDA graph is being captured on its stream,
- * runtimes whose device memory belongs to their own pool allocator, latency-bound loops.
+ * same order), with no allocation and no context. It is for callers that cannot allocate
+ * device memory: a host runtime whose device memory all belongs to its own pool allocator
+ * (CUDA.jl's pool, PyTorch's caching allocator), where a hidden cudaMalloc competes with the
+ * pool, and time-stepping loops that must not stall, since cudaFree synchronises the device.
  * No counterpart in the reference. Its scratch is a fixed file-scope device array
  * (512 blocks x 8 fields x 3 doubles = 96 KiB) that every GPU loading this library keeps
- * until exit; nf > 8 returns BB_ERR_ARG. The first call on a device looks up that array's
- * device address (cudaGetSymbolAddress), so make it before any stream capture. All calls
- * share the array: calls that overlap on the GPU (different streams, no ordering) race.
- * Stream-ordered; does not synchronise. */
+ * until exit; nf > 8 returns BB_ERR_ARG. The first call on a device (and the first after a
+ * cudaDeviceReset) looks up that array's device address with cudaGetSymbolAddress, so make
+ * that call before any stream capture. All calls share the array: calls that overlap on the
+ * GPU (different streams, no ordering between them) race. Stream-ordered; does not
+ * synchronise. A launch error it returns is its own, never one left by an earlier call. */
 int bb_norms_noalloc(int N, int64_t K, int nf, int dtype, const void* a, const void* b,
                      double* out_dev, void* stream);
 

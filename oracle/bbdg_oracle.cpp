@@ -341,7 +341,7 @@ void rhs_example(int N, int K, const SV<T, NF>* q, SV<T, NF>* du, const int* Fma
   for (int e = 0; e < K; ++e)
     for (int i = 0; i < NfpT; ++i) uM[(size_t)e * NfpT + i] = q[(size_t)e * Np + Fmask[i]];
 
-  // interface flux loop (3d_wave.jl:43-56, 3d_maxwell.jl:187-209)
+  // interface flux loop (3d_wave.jl:43-56, 3d_maxwell.jl:43-65)
 #pragma omp parallel for num_threads(nthreads) schedule(static)
   for (int e = 0; e < K; ++e)
     for (int i = 0; i < NfpT; ++i) {
@@ -391,7 +391,7 @@ void rhs_example(int N, int K, const SV<T, NF>* q, SV<T, NF>* du, const int* Fma
       flux[gi] = fl;
     }
 
-  // element loop (3d_wave.jl:58-80, 3d_maxwell.jl:211-233)
+  // element loop (3d_wave.jl:58-80, 3d_maxwell.jl:67-89)
 #pragma omp parallel num_threads(nthreads)
   {
     std::vector<V> fxu(Np), fyu(Np), fzu(Np);
@@ -432,7 +432,7 @@ void rhs_example(int N, int K, const SV<T, NF>* q, SV<T, NF>* du, const int* Fma
         if constexpr (NF == 4)
           due[i] = due[i] - vol;  // wave: du -= ... (3d_wave.jl:76)
         else
-          due[i] = due[i] + vol;  // Maxwell: du += ... (3d_maxwell.jl:229); advection :38-40
+          due[i] = due[i] + vol;  // Maxwell: du += ... (3d_maxwell.jl:85); advection :38-40
       }
       if constexpr (NF == 1)
         for (int i = 0; i < Np; ++i) due[i] = V::zero() - due[i];  // du = -du / J (:41)

@@ -145,7 +145,7 @@ def test_lj_constants(oracle_cpu, bb):
 @pytest.mark.parametrize("phys", [0, 1])
 @pytest.mark.parametrize("tau", [0.0, 1.0])
 def test_example_analytic_solution(oracle_cpu, bb, phys, tau):
-    """The examples' end check (3d_wave.jl:140-145, 3d_maxwell.jl:288-295): L-inf error of
+    """The examples' end check (3d_wave.jl:140-145, 3d_maxwell.jl:141-150): L-inf error of
     the discrete solution vs the analytic standing wave at T = 0.05, N = 7, 4^3 hex mesh."""
     m = bb.uniform_tet_mesh(4)
     N = 7

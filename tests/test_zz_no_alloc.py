@@ -1,12 +1,13 @@
 """bb_norms_noalloc: the allocation-free variant of the FP64 norm reduction.
 
-Some callers cannot allocate device memory (a stream being captured into a CUDA graph, a
-runtime whose device memory belongs to its own pool, a latency-bound loop). This entry point
-keeps its partial sums in a fixed file-scope device array instead of context scratch and
-writes its result to a device buffer the caller passes. The test calls it through the C ABI
-twice in a row and compares each result with bb_norms, the allocating entry point, within
-the reduction tolerance (1e-12 relative; the two differ only in summation order). This file
-is collected last, and it builds everything it uses, so it also runs alone.
+Some callers cannot allocate device memory: a host runtime whose device memory belongs to its
+own pool allocator (CUDA.jl's pool, PyTorch's caching allocator), or a stepping loop that
+must not stall on cudaFree. This entry point keeps its partial sums in a fixed file-scope
+device array instead of context scratch and writes its result to a device buffer the caller
+passes. The test calls it through the C ABI twice in a row and compares each result with
+bb_norms, the allocating entry point, within the reduction tolerance (1e-12 relative; the two
+differ only in summation order). This file is collected last, and it builds everything it
+uses, so it also runs alone.
 """
 import ctypes
 
@@ -52,3 +53,24 @@ def test_norms_noalloc_rejects_too_many_fields(cuda, bb):
     rc = L.bb_norms_noalloc(1, 2, 9, _lib.BB_F64, ctypes.c_void_p(a.data_ptr()), None,
                             ctypes.c_void_p(out.data_ptr()), None)
     assert rc == _lib.BB_ERR_ARG
+
+
+def test_norms_noalloc_without_b_gives_zero_difference_sums(cuda, bb):
+    import torch
+    from bbdg import _lib
+    from bbdg.context import get_context
+    L = _lib.load()
+    ctx = get_context(0)
+    N, K, nf = 3, 777, 2
+    a = torch.tensor(np.random.default_rng(7).standard_normal((nf, K, bb.np3(N))),
+                     dtype=torch.float64, device=cuda)
+    want = (ctypes.c_double * (3 * nf))()
+    assert L.bb_norms(ctx.handle, N, K, nf, _lib.BB_F64, ctypes.c_void_p(a.data_ptr()), None,
+                      want, None) == 0
+    out = torch.full((3 * nf,), float("nan"), dtype=torch.float64, device=cuda)
+    assert L.bb_norms_noalloc(N, K, nf, _lib.BB_F64, ctypes.c_void_p(a.data_ptr()), None,
+                              ctypes.c_void_p(out.data_ptr()), None) == 0
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().reshape(nf, 3)
+    np.testing.assert_allclose(got[:, 0], np.array(want[:]).reshape(nf, 3)[:, 0], rtol=1e-12)
+    assert np.all(got[:, 1:] == 0)
