@@ -273,6 +273,17 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
     tma_load(slot_geo(s), ggeo + e0 * BB_GEO_STRIDE, L::GEOBYTES, &bar[s]);
     tma_load(slot_conn(s), gconn + e0 * 4, L::CONNBYTES, &bar[s]);
   };
+  // tile t's q, geometry, connectivity and res -> L2, two tiles before they are copied in
+  auto prefetch_tile = [=](int64_t t) {
+    const int64_t e0 = t * EPB;
+#pragma unroll
+    for (int m = 0; m < NF; ++m) {
+      l2_prefetch(gq + ((size_t)m * K + e0) * NP, EPB * NP * 4);
+      if (stage) l2_prefetch(gres + ((size_t)m * K + e0) * NP, EPB * NP * 4);
+    }
+    l2_prefetch(ggeo + e0 * BB_GEO_STRIDE, L::GEOBYTES);
+    l2_prefetch(gconn + e0 * 4, L::CONNBYTES);
+  };
   auto issue_res = [=](int64_t t) {
     const int64_t e0 = t * EPB;
     mbar_expect_tx(&bar[2], L::QBYTES);
@@ -372,6 +383,7 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
     ++iss0;
     if (stage) issue_res(t0), ++iss2;
     if (t0 + gridDim.x < ntiles) issue_main(t0 + gridDim.x, 1), ++iss1;
+    if (t0 + 2 * (int64_t)gridDim.x < ntiles) prefetch_tile(t0 + 2 * (int64_t)gridDim.x);
   }
   uint32_t ph = 0u;  // bit b: parity of the phase barrier b waits for next (element threads)
   const float rkA = P.rkA, rkB = P.rkB, dt = P.dt, tau = P.tau;
@@ -495,6 +507,7 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
             else ++iss1;
           }
           if (stage) issue_res(tile), ++iss2;
+          if (tnext + gridDim.x < ntiles) prefetch_tile(tnext + gridDim.x);
         }
       }
       const int c = tid - NTE;

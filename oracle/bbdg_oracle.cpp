@@ -306,7 +306,10 @@ struct LiftScratch {
 //   nJ[(e*NfpT + i)*3 + c] = (nxJ, nyJ, nzJ)[c] at face node i of element e
 //   Fmask[i]  volume index of face node i (i < 4*Nfp, faces in reference order)
 //   mapP[e*NfpT + i] global face-node index of the neighbour node (e' * NfpT + i')
-//   J  the constant Jacobian md.J[1,1]
+//   J  the constant Jacobian md.J[1,1]; Jall (may be null) the per-element Jacobian. The
+//      examples divide by md.J[1,1] (3d_wave.jl:82-83: "md.J is constant" on their uniform
+//      meshes); with Jall the division is by each element's own J, which is the same on a
+//      uniform mesh and the right one on a mesh whose elements differ in size.
 // --------------------------------------------------------------------------------------
 
 // examples/3d_wave.jl:20-33
@@ -329,7 +332,8 @@ inline void maxwell_fluxes(const SV<T, 6>& q, SV<T, 6>& fx, SV<T, 6>& fy, SV<T, 
 
 template <class T, int NF>
 void rhs_example(int N, int K, const SV<T, NF>* q, SV<T, NF>* du, const int* Fmask,
-                 const int64_t* mapP, const T* geo9, const T* nJ, T J, T tau, int nthreads) {
+                 const int64_t* mapP, const T* geo9, const T* nJ, T J, const T* Jall, T tau,
+                 int nthreads) {
   const int Np = np3(N);
   const int NfpT = 4 * np2(N);
   const Offsets o = make_offsets(N);
@@ -436,8 +440,9 @@ void rhs_example(int N, int K, const SV<T, NF>* q, SV<T, NF>* du, const int* Fma
       }
       if constexpr (NF == 1)
         for (int i = 0; i < Np; ++i) due[i] = V::zero() - due[i];  // du = -du / J (:41)
-      // du ./= J[1,1]  (3d_wave.jl:83)
-      for (int i = 0; i < Np; ++i) due[i] = due[i] / J;
+      // du ./= J[1,1]  (3d_wave.jl:83), or the element's own J
+      const T Je = Jall ? Jall[e] : J;
+      for (int i = 0; i < Np; ++i) due[i] = due[i] / Je;
     }
   }
 }
@@ -453,13 +458,13 @@ const double RK4B[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 136
 
 template <class T, int NF>
 void lsrk_run(int N, int K, SV<T, NF>* q, SV<T, NF>* res, const int* Fmask,
-              const int64_t* mapP, const T* geo9, const T* nJ, T J, T tau, T dt, int nsteps,
-              int nthreads) {
+              const int64_t* mapP, const T* geo9, const T* nJ, T J, const T* Jall, T tau, T dt,
+              int nsteps, int nthreads) {
   const size_t n = (size_t)np3(N) * K;
   std::vector<SV<T, NF>> rhs(n);
   for (int step = 0; step < nsteps; ++step)
     for (int s = 0; s < 5; ++s) {
-      rhs_example<T, NF>(N, K, q, rhs.data(), Fmask, mapP, geo9, nJ, J, tau, nthreads);
+      rhs_example<T, NF>(N, K, q, rhs.data(), Fmask, mapP, geo9, nJ, J, Jall, tau, nthreads);
       const T a = T(RK4A[s]), b = T(RK4B[s]);
 #pragma omp parallel for num_threads(nthreads) schedule(static)
       for (long long m = 0; m < (long long)n; ++m)
@@ -541,29 +546,29 @@ void oracle_lift_f32(int N, int K, const float* x, float* out, int nthreads) {
 // examples/3d_advec_scalar.jl). q/du are AoS Np x K of SVector{nf}.
 int oracle_rhs_f64(int phys, int N, int K, const double* q, double* du, const int* Fmask,
                    const int64_t* mapP, const double* geo9, const double* nJ, double J,
-                   double tau, int nthreads) {
+                   const double* Jall, double tau, int nthreads) {
   if (phys == 0)
     rhs_example<double, 4>(N, K, (const SV<double, 4>*)q, (SV<double, 4>*)du, Fmask, mapP,
-                           geo9, nJ, J, tau, nthreads);
+                           geo9, nJ, J, Jall, tau, nthreads);
   else if (phys == 2)
     rhs_example<double, 1>(N, K, (const SV<double, 1>*)q, (SV<double, 1>*)du, Fmask, mapP,
-                           geo9, nJ, J, tau, nthreads);
+                           geo9, nJ, J, Jall, tau, nthreads);
   else if (phys == 1)
     rhs_example<double, 6>(N, K, (const SV<double, 6>*)q, (SV<double, 6>*)du, Fmask, mapP,
-                           geo9, nJ, J, tau, nthreads);
+                           geo9, nJ, J, Jall, tau, nthreads);
   else
     return 1;
   return 0;
 }
 int oracle_rhs_f32(int phys, int N, int K, const float* q, float* du, const int* Fmask,
                    const int64_t* mapP, const float* geo9, const float* nJ, float J,
-                   float tau, int nthreads) {
+                   const float* Jall, float tau, int nthreads) {
   if (phys == 0)
-    rhs_example<float, 4>(N, K, (const SV<float, 4>*)q, (SV<float, 4>*)du, Fmask, mapP, geo9, nJ, J, tau, nthreads);
+    rhs_example<float, 4>(N, K, (const SV<float, 4>*)q, (SV<float, 4>*)du, Fmask, mapP, geo9, nJ, J, Jall, tau, nthreads);
   else if (phys == 2)
-    rhs_example<float, 1>(N, K, (const SV<float, 1>*)q, (SV<float, 1>*)du, Fmask, mapP, geo9, nJ, J, tau, nthreads);
+    rhs_example<float, 1>(N, K, (const SV<float, 1>*)q, (SV<float, 1>*)du, Fmask, mapP, geo9, nJ, J, Jall, tau, nthreads);
   else if (phys == 1)
-    rhs_example<float, 6>(N, K, (const SV<float, 6>*)q, (SV<float, 6>*)du, Fmask, mapP, geo9, nJ, J, tau, nthreads);
+    rhs_example<float, 6>(N, K, (const SV<float, 6>*)q, (SV<float, 6>*)du, Fmask, mapP, geo9, nJ, J, Jall, tau, nthreads);
   else
     return 1;
   return 0;
@@ -571,28 +576,28 @@ int oracle_rhs_f32(int phys, int N, int K, const float* q, float* du, const int*
 
 int oracle_lsrk_f64(int phys, int N, int K, double* q, double* res, const int* Fmask,
                     const int64_t* mapP, const double* geo9, const double* nJ, double J,
-                    double tau, double dt, int nsteps, int nthreads) {
+                    const double* Jall, double tau, double dt, int nsteps, int nthreads) {
   if (phys == 0)
-    lsrk_run<double, 4>(N, K, (SV<double, 4>*)q, (SV<double, 4>*)res, Fmask, mapP, geo9, nJ, J, tau, dt, nsteps, nthreads);
+    lsrk_run<double, 4>(N, K, (SV<double, 4>*)q, (SV<double, 4>*)res, Fmask, mapP, geo9, nJ, J, Jall, tau, dt, nsteps, nthreads);
   else if (phys == 2)
-    lsrk_run<double, 1>(N, K, (SV<double, 1>*)q, (SV<double, 1>*)res, Fmask, mapP, geo9, nJ, J, tau, dt, nsteps, nthreads);
+    lsrk_run<double, 1>(N, K, (SV<double, 1>*)q, (SV<double, 1>*)res, Fmask, mapP, geo9, nJ, J, Jall, tau, dt, nsteps, nthreads);
   else if (phys == 1)
-    lsrk_run<double, 6>(N, K, (SV<double, 6>*)q, (SV<double, 6>*)res, Fmask, mapP, geo9, nJ, J, tau, dt, nsteps, nthreads);
+    lsrk_run<double, 6>(N, K, (SV<double, 6>*)q, (SV<double, 6>*)res, Fmask, mapP, geo9, nJ, J, Jall, tau, dt, nsteps, nthreads);
   else
     return 1;
   return 0;
 }
 int oracle_lsrk_f32(int phys, int N, int K, float* q, float* res, const int* Fmask,
                     const int64_t* mapP, const float* geo9, const float* nJ, float J,
-                    float tau, float dt, int nsteps, int nthreads) {
+                    const float* Jall, float tau, float dt, int nsteps, int nthreads) {
   if (phys == 0)
-    lsrk_run<float, 4>(N, K, (SV<float, 4>*)q, (SV<float, 4>*)res, Fmask, mapP, geo9, nJ, J,
+    lsrk_run<float, 4>(N, K, (SV<float, 4>*)q, (SV<float, 4>*)res, Fmask, mapP, geo9, nJ, J, Jall,
                        tau, dt, nsteps, nthreads);
   else if (phys == 2)
-    lsrk_run<float, 1>(N, K, (SV<float, 1>*)q, (SV<float, 1>*)res, Fmask, mapP, geo9, nJ, J,
+    lsrk_run<float, 1>(N, K, (SV<float, 1>*)q, (SV<float, 1>*)res, Fmask, mapP, geo9, nJ, J, Jall,
                        tau, dt, nsteps, nthreads);
   else if (phys == 1)
-    lsrk_run<float, 6>(N, K, (SV<float, 6>*)q, (SV<float, 6>*)res, Fmask, mapP, geo9, nJ, J,
+    lsrk_run<float, 6>(N, K, (SV<float, 6>*)q, (SV<float, 6>*)res, Fmask, mapP, geo9, nJ, J, Jall,
                        tau, dt, nsteps, nthreads);
   else
     return 1;

@@ -28,12 +28,12 @@ def lib():
             getattr(L, name).argtypes = [I, _P, _P]
         L.oracle_lift_f64.argtypes = [I, I, _P, _P, I]
         L.oracle_lift_f32.argtypes = [I, I, _P, _P, I]
-        L.oracle_rhs_f64.argtypes = [I, I, I, _P, _P, _P, _P, _P, _P, D, D, I]
-        L.oracle_rhs_f32.argtypes = [I, I, I, _P, _P, _P, _P, _P, _P, F, F, I]
+        L.oracle_rhs_f64.argtypes = [I, I, I, _P, _P, _P, _P, _P, _P, D, _P, D, I]
+        L.oracle_rhs_f32.argtypes = [I, I, I, _P, _P, _P, _P, _P, _P, F, _P, F, I]
         L.oracle_rhs_f64.restype = I
         L.oracle_rhs_f32.restype = I
-        L.oracle_lsrk_f64.argtypes = [I, I, I, _P, _P, _P, _P, _P, _P, D, D, D, I, I]
-        L.oracle_lsrk_f32.argtypes = [I, I, I, _P, _P, _P, _P, _P, _P, F, F, F, I, I]
+        L.oracle_lsrk_f64.argtypes = [I, I, I, _P, _P, _P, _P, _P, _P, D, _P, D, D, I, I]
+        L.oracle_lsrk_f32.argtypes = [I, I, I, _P, _P, _P, _P, _P, _P, F, _P, F, F, I, I]
         L.oracle_lsrk_f64.restype = I
         L.oracle_lsrk_f32.restype = I
         _lib = L
@@ -111,13 +111,22 @@ def aos_to_soa(q: np.ndarray) -> np.ndarray:
     return np.ascontiguousarray(np.transpose(q, (2, 0, 1)))
 
 
+def _jall(md, dt_, per_element_J):
+    """Per-element Jacobians (kept alive by the caller) or None for the examples' md.J[1,1]."""
+    if not per_element_J:
+        return None, None
+    a = np.ascontiguousarray(md.Jall, dtype=dt_)
+    return a, _ptr(a)
+
+
 def rhs(phys: int, N: int, q_soa: np.ndarray, md, tau: float = 0.0,
-        nthreads: int = 0) -> np.ndarray:
+        nthreads: int = 0, per_element_J: bool = False) -> np.ndarray:
     """Example right-hand side (wave phys=0, Maxwell phys=1, scalar advection phys=2,
     examples/3d_advec_scalar.jl) on SoA state (nf, K, Np).
 
     tau <= 0 evaluates the examples' flux as written; tau > 0 scales the penalty by the
-    face Jacobian (upwind penalty tau).
+    face Jacobian (upwind penalty tau). per_element_J divides by each element's own J instead
+    of the examples' md.J[1,1] (the two agree on uniform meshes).
     """
     nthreads = nthreads or max_threads()
     dt_ = q_soa.dtype
@@ -127,14 +136,15 @@ def rhs(phys: int, N: int, q_soa: np.ndarray, md, tau: float = 0.0,
     nJ = np.ascontiguousarray(md.nJ, dtype=dt_)
     K = q.shape[0]
     fn = lib().oracle_rhs_f64 if dt_ == np.float64 else lib().oracle_rhs_f32
+    jall, jp = _jall(md, dt_, per_element_J)
     rc = fn(phys, N, K, _ptr(q), _ptr(du), _ptr(md.Fmask), _ptr(md.mapP), _ptr(geo9),
-            _ptr(nJ), float(md.J), float(tau), nthreads)
+            _ptr(nJ), float(md.J), jp, float(tau), nthreads)
     assert rc == 0
     return aos_to_soa(du)
 
 
 def lsrk(phys: int, N: int, q_soa: np.ndarray, md, dt: float, nsteps: int, tau: float = 0.0,
-         nthreads: int = 0, res_soa: np.ndarray | None = None):
+         nthreads: int = 0, res_soa: np.ndarray | None = None, per_element_J: bool = False):
     """Advance nsteps LSRK45 steps; returns (q, res) in SoA layout."""
     nthreads = nthreads or max_threads()
     dt_ = q_soa.dtype
@@ -144,7 +154,8 @@ def lsrk(phys: int, N: int, q_soa: np.ndarray, md, dt: float, nsteps: int, tau: 
     nJ = np.ascontiguousarray(md.nJ, dtype=dt_)
     K = q.shape[0]
     fn = lib().oracle_lsrk_f64 if dt_ == np.float64 else lib().oracle_lsrk_f32
+    jall, jp = _jall(md, dt_, per_element_J)
     rc = fn(phys, N, K, _ptr(q), _ptr(res), _ptr(md.Fmask), _ptr(md.mapP), _ptr(geo9),
-            _ptr(nJ), float(md.J), float(tau), float(dt), nsteps, nthreads)
+            _ptr(nJ), float(md.J), jp, float(tau), float(dt), nsteps, nthreads)
     assert rc == 0
     return aos_to_soa(q), aos_to_soa(res)

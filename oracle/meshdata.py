@@ -103,3 +103,37 @@ def build(mesh, N: int) -> MeshData:
     return MeshData(N=N, K=K, Fmask=Fm, mapP=np.ascontiguousarray(mapP.reshape(-1), np.int64),
                     geo9=np.ascontiguousarray(geo9), nJ=np.ascontiguousarray(nJ),
                     J=float(Jall[0]), Jall=Jall)
+
+
+@dataclass
+class LatticeMesh:
+    """Vertex arrays of an affine tetrahedral mesh on a periodic vertex lattice: the fields
+    `build` reads (K, n, EVI lattice coordinates, EVX physical coordinates)."""
+    n: int
+    K: int
+    h: float
+    EVI: np.ndarray
+    EVX: np.ndarray
+
+
+_EVEN_PERMS = [p for p in __import__("itertools").permutations(range(4))
+               if sum(p[i] > p[j] for i in range(4) for j in range(i + 1, 4)) % 2 == 0]
+
+
+def scrambled(mesh, seed: int, jitter: float = 0.15) -> LatticeMesh:
+    """A mesh that is not the generator's own: each element's vertices re-listed by a random
+    even permutation (so faces meet in every orientation), the elements shuffled, and every
+    lattice vertex moved by a random offset of up to jitter*h per coordinate (the same offset
+    for a vertex and its periodic images, so the mesh stays conforming and periodic; the
+    elements stay affine but differ in size and shape)."""
+    rng = np.random.default_rng(seed)
+    K, n, h = mesh.K, mesh.n, 2.0 / mesh.n
+    perm = np.array(_EVEN_PERMS)[rng.integers(0, len(_EVEN_PERMS), K)]     # (K, 4)
+    EVI = np.take_along_axis(mesh.EVI, perm[:, :, None], axis=1)
+    order = rng.permutation(K)
+    EVI = EVI[order]
+    w = np.mod(EVI, n)
+    vid = w[..., 0] + n * (w[..., 1] + n * w[..., 2])
+    delta = rng.uniform(-jitter * h, jitter * h, (n ** 3, 3))
+    EVX = -1.0 + h * EVI.astype(np.float64) + delta[vid]
+    return LatticeMesh(n=n, K=K, h=h, EVI=np.ascontiguousarray(EVI), EVX=EVX)
