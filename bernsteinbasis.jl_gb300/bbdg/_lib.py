@@ -57,6 +57,7 @@ SIGNATURES = {
     "bb_stage_tile_bytes": (_I, [_I, _I, _I, _I, ctypes.POINTER(_I64), ctypes.POINTER(_I)]),
     "bb_rhs": (_I, [_P, _P, _P, _P]),
     "bb_lsrk_run": (_I, [_P, _D, _I, _P, _P, _I, _P]),
+    "bb_solver_check": (_I, [_P, _P]),
     "bb_lsrk_run_host": (_I, [_P, _D, _I, _P, _P, _P, _P, _I, _P]),
     "bb_norms": (_I, [_P, _I, _I64, _I, _I, _P, _P, ctypes.POINTER(_D), _P]),
     "bb_mass_norms": (_I, [_P, _I, _I64, _I, _I, _P, _P, _P, ctypes.POINTER(_D), _P]),
@@ -82,6 +83,8 @@ SIGNATURES.update({
     "bb_gemm_bf16": (_I, [_P, _I64, _I, _I, _P, _P, ctypes.c_float, _P, _I, _P, _P, _P, _P, _P,
                           _I, _I, _I, _P]),
     "bb_device_status": (_I, [_P, _P, ctypes.POINTER(_I)]),
+    "bb_ctx_set_wait_limit": (_I, [_P, ctypes.c_uint32]),
+    "bb_ctx_set_test_fault": (_I, [_P, _I]),
     "bb_transpose_bf16": (_I, [_P, _I64, _I, _P, _P, _P]),
     "bb_mlp_create": (_I, [_P, _I, _I, _I, _I, _I64, ctypes.c_uint64, ctypes.POINTER(_P)]),
     "bb_mlp_destroy": (_I, [_P]),

@@ -33,6 +33,23 @@ class Context:
     def check(self, rc: int, what: str = "") -> None:
         _lib.check(rc, self.handle, what)
 
+    def set_wait_limit(self, polls: int = 0) -> None:
+        """Polls before a device-side mbarrier wait gives up (0: the default, about 1 s)."""
+        self.check(_lib.load().bb_ctx_set_wait_limit(self.handle, int(polls)),
+                   "bb_ctx_set_wait_limit")
+
+    def set_test_fault(self, mode: int) -> None:
+        """Test only: 1 leaves one bulk copy out so that a bounded wait runs out; 0 = off."""
+        self.check(_lib.load().bb_ctx_set_test_fault(self.handle, int(mode)),
+                   "bb_ctx_set_test_fault")
+
+    def device_status(self, stream=None) -> int:
+        """Reads and clears the context's device status word (GEMM and closure kernels)."""
+        out = ctypes.c_int(0)
+        self.check(_lib.load().bb_device_status(self.handle, stream_handle(stream),
+                                                ctypes.byref(out)), "bb_device_status")
+        return out.value
+
     def close(self) -> None:
         if self.handle:
             _lib.load().bb_ctx_destroy(self.handle)

@@ -126,6 +126,13 @@ class DGSolver:
                                                ptr(res), int(bool(graph)),
                                                stream_handle(stream)), "bb_lsrk_run")
 
+    def check(self, stream=None) -> None:
+        """Waits for the stream and raises BBError if a kernel of this solver reported a
+        problem since the last check (BB_ERR_TIMEOUT: a bounded device wait ran out;
+        BB_ERR_DEVICE: corrupt connectivity)."""
+        self.ctx.check(_lib.load().bb_solver_check(self.handle, stream_handle(stream)),
+                       "bb_solver_check")
+
     def run_host(self, q_host_in: torch.Tensor, q_host_out: torch.Tensor, q_dev: torch.Tensor,
                  res_dev: torch.Tensor, dt: float, nsteps: int, graph: bool = True,
                  stream=None) -> None:

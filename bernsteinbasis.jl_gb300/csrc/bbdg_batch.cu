@@ -129,6 +129,7 @@ struct bb_batch {
   cudaStream_t side[kSideStreams] = {};
   cudaEvent_t fork_ev = nullptr, join_ev[kSideStreams] = {};
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  int64_t g_epoch = -1;  // the context's config_epoch the graphs were captured under
 };
 
 namespace {
@@ -252,6 +253,8 @@ int launch_fast_lane(bb_batch* b, int p, int s, int par, cudaStream_t st) {
   P.status = b->d_status;
   FastLaunch fl;
   fl.num_sms = b->ctx->num_sms;
+  fl.wait_iters = b->ctx->wait_iters;
+  fl.fault = b->ctx->test_fault;
   const int rc = bb_fast_launch(b->fast[p], fl, P, st);
   if (rc) return bb_fail(b->ctx, rc, "stage_fast_kernel launch: %s", cudaGetErrorString(cudaGetLastError()));
   b->ctx->launches++;
@@ -318,6 +321,10 @@ int batch_extract(bb_batch* b, cudaStream_t st) {
 template <class T>
 int batch_run_t(bb_batch* b, int nsteps, int use_graph, cudaStream_t st) {
   bb_ctx* ctx = b->ctx;
+  if (b->g_epoch != ctx->config_epoch) {
+    drop_batch_graphs(b);
+    b->g_epoch = ctx->config_epoch;
+  }
   if (b->dirty) {
     drop_batch_graphs(b);
     int rc = build_desc<T>(b);

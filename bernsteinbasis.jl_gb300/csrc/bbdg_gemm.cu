@@ -66,9 +66,9 @@ __device__ __forceinline__ bool mbar_test(uint64_t* b, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait (about a second), false on time-out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
-  for (uint32_t it = 0; it < (1u << 24); ++it) {
+// Bounded wait: `limit` polls (2^24, about a second, by default), false on time-out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, uint32_t limit) {
+  for (uint32_t it = 0; it < limit; ++it) {
     if (mbar_test(b, parity)) return true;
     if (it > 64) __nanosleep(64);
   }
@@ -369,6 +369,7 @@ __global__ void __launch_bounds__(GemmCfg<BN>::THREADS, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   volatile int* abort_flag = &s_abort;
+  const uint32_t wlim = ep.wait_iters ? ep.wait_iters : (1u << 24);
   const int total = ts.total();
 
   if (warp == 0) {
@@ -380,13 +381,16 @@ __global__ void __launch_bounds__(GemmCfg<BN>::THREADS, 1)
         ts.decode(tile, mt, nt, kt0, nkt);
         for (int kt = 0; kt < nkt; ++kt, ++it) {
           const int s = it % C::STAGES;
-          if (!mbar_wait(&empty[s], ((it / C::STAGES) & 1) ^ 1)) {
+          if (!mbar_wait(&empty[s], ((it / C::STAGES) & 1) ^ 1, wlim)) {
             atomicOr(ep.status, 2);
             *abort_flag = 1;
             break;
           }
           unsigned char* st = smem + s * C::STAGE_BYTES;
           mbar_expect_tx(&full[s], C::STAGE_BYTES);
+          // test-only fault mode: the stage's barrier is armed but its copies are left out,
+          // so the MMA issuer's bounded wait on it runs out
+          if (ep.fault == 1 && it == 1) continue;
           tma_load_2d(st, &tmA, (kt0 + kt) * C::BK, mt * C::BM, &full[s]);
           tma_load_2d(st + C::A_BYTES, &tmB, (kt0 + kt) * C::BK, nt * BN, &full[s]);
         }
@@ -402,7 +406,7 @@ __global__ void __launch_bounds__(GemmCfg<BN>::THREADS, 1)
         int mt, nt, kt0, nkt;
         ts.decode(tile, mt, nt, kt0, nkt);
         const int a = local & 1;
-        if (!mbar_wait(&tempty[a], ((local >> 1) & 1) ^ 1)) {
+        if (!mbar_wait(&tempty[a], ((local >> 1) & 1) ^ 1, wlim)) {
           atomicOr(ep.status, 2);
           *abort_flag = 1;
           break;
@@ -412,7 +416,7 @@ __global__ void __launch_bounds__(GemmCfg<BN>::THREADS, 1)
         bool ok = true;
         for (int kt = 0; kt < nkt; ++kt, ++it) {
           const int s = it % C::STAGES;
-          if (!mbar_wait(&full[s], (it / C::STAGES) & 1)) {
+          if (!mbar_wait(&full[s], (it / C::STAGES) & 1, wlim)) {
             atomicOr(ep.status, 2);
             *abort_flag = 1;
             ok = false;
@@ -447,7 +451,7 @@ __global__ void __launch_bounds__(GemmCfg<BN>::THREADS, 1)
       const int a = local & 1;
       int ok = 0;
       if (lane == 0) {
-        ok = !flag_set(abort_flag) && mbar_wait(&tfull[a], (local >> 1) & 1);
+        ok = !flag_set(abort_flag) && mbar_wait(&tfull[a], (local >> 1) & 1, wlim);
         if (!ok && !flag_set(abort_flag)) {
           atomicOr(ep.status, 2);
           *abort_flag = 1;
@@ -496,11 +500,11 @@ __global__ void __launch_bounds__(GemmCfg<BN>::THREADS, 1)
   __syncthreads();
   if (threadIdx.x == 0) {
     // MMAs still in flight (normal exit: none) must finish before TMEM is freed
-    if (!mbar_wait(mdone, 0)) atomicOr(ep.status, 2);
+    if (!mbar_wait(mdone, 0, wlim)) atomicOr(ep.status, 2);
     if (flag_set(abort_flag)) {
       // copies issued but never consumed land before the CTA exits
       for (int it = s_consumed; it < s_issued; ++it)
-        mbar_wait(&full[it % C::STAGES], (it / C::STAGES) & 1);
+        mbar_wait(&full[it % C::STAGES], (it / C::STAGES) & 1, wlim);
     }
   }
   tc_fence_before();
@@ -608,6 +612,8 @@ int bb_gemm_launch(bb_ctx* ctx, int64_t M, int N, int K, const void* A, const vo
   if (((uintptr_t)A | (uintptr_t)B) & 15)
     return bb_fail(ctx, BB_ERR_ARG, "GEMM operands must be 16-byte aligned");
   if (M > ((int64_t)1 << 30) / 2) return bb_fail(ctx, BB_ERR_ARG, "GEMM M too large");
+  ep.wait_iters = ctx->wait_iters;
+  ep.fault = ctx->test_fault;
   int rc = get_encoder(ctx);
   if (rc) return rc;
   CUtensorMap ta;

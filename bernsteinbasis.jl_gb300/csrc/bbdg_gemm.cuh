@@ -30,6 +30,8 @@ struct GemmEpilogue {
   int ldc, ldt;
   int kt_per;   // split-K: K blocks of 64 per CTA (0 = no split); split outputs add into Cf
   int* status;  // device error word: bit 1 = a pipeline wait ran out
+  uint32_t wait_iters;  // polls of a bounded mbarrier wait before it gives up (0 = 2^24)
+  int fault;            // test only: 1 = the second operand copy is left out
 };
 
 // Launches the GEMM on `st` (A, B device pointers, 16-byte aligned, K % 8 == 0).

@@ -106,6 +106,9 @@ struct bb_ctx {
   size_t red_cap = 0;          // entries
   double* h_red = nullptr;     // pinned host mirror
   int* d_status = nullptr;     // device error word of the GEMM / closure kernels
+  uint32_t wait_iters = 0;     // bound of the device-side mbarrier waits (0 = 2^24 polls)
+  int test_fault = 0;          // test-only fault mode (bb_ctx_set_test_fault)
+  int64_t config_epoch = 0;    // bumped when either changes: captured graphs are rebuilt
 };
 
 // Error helpers -----------------------------------------------------------------------

@@ -110,7 +110,8 @@ struct Lift4 {
 
 template <int N>
 __global__ void __launch_bounds__(32) lift4_kernel(int64_t K, const float* __restrict__ x,
-                                                   float* __restrict__ out, int* status) {
+                                                   float* __restrict__ out, int* status,
+                                                   uint32_t wait_iters) {
   using L = Lift4<N>;
   constexpr int NP = L::NP, NFP = L::NFP, NPS = L::NPS, NFPP = L::NFPP, EPW = L::EPW;
   constexpr int INW = L::INW, NV4 = L::NV4;
@@ -150,9 +151,11 @@ __global__ void __launch_bounds__(32) lift4_kernel(int64_t K, const float* __res
         "l"(x + tile * EPW * 4 * NFP), "r"(bytes), "r"(lf_saddr(bar))
         : "memory");
   };
-  // bounded wait for the bulk copy with the given phase parity (about a second at most)
+  // bounded wait for the bulk copy with the given phase parity (2^24 polls, about a second,
+  // unless the context sets another limit)
+  const uint32_t wlim = wait_iters ? wait_iters : (1u << 24);
   auto wait_in = [&](uint32_t parity) {
-    for (uint32_t it = 0; it < (1u << 24); ++it) {
+    for (uint32_t it = 0; it < wlim; ++it) {
       uint32_t ok;
       asm volatile(
           "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
@@ -204,7 +207,7 @@ __global__ void __launch_bounds__(32) lift4_kernel(int64_t K, const float* __res
     } else {
       if (!wait_in(ph)) {
         if (t == 0) {
-          atomicOr(status, 1);
+          atomicOr(status, 2);
           wait_in(ph);  // let the copy in flight land before the block exits (bounded)
         }
         return;
@@ -246,7 +249,7 @@ int launch_lift4(bb_ctx* ctx, int64_t K, const void* x, void* out, cudaStream_t 
   if (per_sm < 1) return bb_fail(ctx, BB_ERR_ARG, "lift tile does not fit");
   const int64_t ntile = (K + L::EPW - 1) / L::EPW;
   const int grid = (int)std::min<int64_t>(ntile, (int64_t)per_sm * ctx->num_sms);
-  kern<<<grid, 32, L::SMEM, st>>>(K, (const float*)x, (float*)out, status);
+  kern<<<grid, 32, L::SMEM, st>>>(K, (const float*)x, (float*)out, status, ctx->wait_iters);
   return bb_check_launch(ctx, "lift4_kernel");
 }
 

@@ -44,6 +44,22 @@ int bb_device_status_error(bb_ctx* ctx, int word) {
                  word);
 }
 
+extern "C" int bb_ctx_set_wait_limit(bb_ctx* ctx, uint32_t polls) {
+  if (!ctx) return BB_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  ctx->wait_iters = polls;
+  ++ctx->config_epoch;
+  return BB_OK;
+}
+
+extern "C" int bb_ctx_set_test_fault(bb_ctx* ctx, int mode) {
+  if (!ctx || mode < 0 || mode > 1) return BB_ERR_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  ctx->test_fault = mode;
+  ++ctx->config_epoch;
+  return BB_OK;
+}
+
 extern "C" int bb_version(void) { return 10000; }
 
 extern "C" int bb_ctx_create(int device, bb_ctx** out) {

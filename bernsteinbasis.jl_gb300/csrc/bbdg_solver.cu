@@ -78,6 +78,7 @@ struct bb_solver {
   void* g_res = nullptr;
   double g_dt = 0.0;
   int g_epb = 0;
+  int64_t g_epoch = -1;  // the context's config_epoch the graphs were captured under
 };
 
 namespace {
@@ -161,6 +162,8 @@ int launch_fast(bb_solver* s, int mode, int stage, double dt, void* q, void* res
   P.status = s->d_status;
   FastLaunch fl;
   fl.num_sms = s->ctx->num_sms;
+  fl.wait_iters = s->ctx->wait_iters;
+  fl.fault = s->ctx->test_fault;
   const int rc = bb_fast_launch(s->fast, fl, P, st);
   if (rc) return bb_fail(s->ctx, rc, "stage_fast_kernel launch: %s", cudaGetErrorString(cudaGetLastError()));
   s->ctx->launches++;
@@ -434,6 +437,13 @@ extern "C" int bb_rhs(bb_solver* s, const void* q, void* rhs, void* stream) {
   return check_status(s, st);
 }
 
+extern "C" int bb_solver_check(bb_solver* s, void* stream) {
+  if (!s) return BB_ERR_ARG;
+  int rc = bb_set_device(s->ctx);
+  if (rc) return rc;
+  return check_status(s, (cudaStream_t)stream);
+}
+
 extern "C" int bb_lsrk_run(bb_solver* s, double dt, int nsteps, void* q, void* res, int use_graph,
                            void* stream) {
   if (!s || !q || !res) return s ? bb_fail(s->ctx, BB_ERR_ARG, "null pointer") : BB_ERR_ARG;
@@ -447,7 +457,9 @@ extern "C" int bb_lsrk_run(bb_solver* s, double dt, int nsteps, void* q, void* r
   rc = launch_extract(s, q, s->trace[0], st);
   if (rc) return rc;
   if (use_graph) {
-    if (s->g_q != q || s->g_res != res || s->g_dt != dt || s->g_epb != s->epb) drop_graphs(s);
+    if (s->g_q != q || s->g_res != res || s->g_dt != dt || s->g_epb != s->epb ||
+        s->g_epoch != s->ctx->config_epoch)
+      drop_graphs(s);
     for (int par = 0; par < 2; ++par)
       if (!s->graph[par]) {
         rc = build_graph(s, dt, q, res, par);
@@ -457,6 +469,7 @@ extern "C" int bb_lsrk_run(bb_solver* s, double dt, int nsteps, void* q, void* r
     s->g_res = res;
     s->g_dt = dt;
     s->g_epb = s->epb;
+    s->g_epoch = s->ctx->config_epoch;
     for (int step = 0; step < nsteps; ++step) {
       BB_CUDA(s->ctx, cudaGraphLaunch(s->graph[step & 1], st));
       s->ctx->launches += 5;

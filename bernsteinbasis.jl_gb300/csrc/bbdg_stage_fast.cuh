@@ -17,6 +17,8 @@ struct FastStageParams {
   const float* geo;      // [K][BB_GEO_STRIDE]
   const int32_t* conn;   // [K][4]
   int* status;
+  uint32_t wait_iters;   // polls of a bounded mbarrier wait before it gives up (0 = 2^24)
+  int fault;             // test only: 1 = one bulk copy is left out (a wait then runs out)
   // volume phase: warp-round g = r * (TPE / 32) + warp forms w(beta) for beta = vstart[g] +
   // lane, lane < vlen[g] (filled by the launcher)
   uint16_t vstart[16];
@@ -25,6 +27,8 @@ struct FastStageParams {
 
 struct FastLaunch {
   int num_sms;
+  uint32_t wait_iters;  // copied into FastStageParams (the context's wait limit)
+  int fault;            // copied into FastStageParams (the context's test-only fault mode)
 };
 
 // Index of the compiled variant for (N, physics, elements per block, threads), 0 = any,

@@ -144,9 +144,10 @@ __device__ __forceinline__ void nbar_sync(int id, int count) {
 __device__ __forceinline__ void nbar_arrive(int id, int count) {
   asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
-// Bounded wait for the phase with the given parity: about a second at most, then false.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (uint32_t it = 0; it < (1u << 24); ++it) {
+// Bounded wait for the phase with the given parity: `limit` polls (2^24, about a second, by
+// default), then false.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
+  for (uint32_t it = 0; it < limit; ++it) {
     if (mbar_test(bar, parity)) return true;
     if (it > 64) __nanosleep(64);
   }
@@ -249,6 +250,7 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
   const int tid = threadIdx.x;
   const int64_t K = P.K;
   const int64_t ntiles = K / EPB;  // the host guarantees K % EPB == 0
+  const uint32_t wlim = P.wait_iters ? P.wait_iters : (1u << 24);
   const bool stage = P.mode != 0;
   // element threads: element le, lane u within the element
   const int le = tid / TPE, u = tid - (tid / TPE) * TPE;
@@ -263,10 +265,13 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
   const float* gres = P.res;
   const float* ggeo = P.geo;
   const int32_t* gconn = P.conn;
-  // tile t's q, geometry and connectivity -> slot s (thread 0 only)
-  auto issue_main = [=](int64_t t, int s) {
+  // tile t's q, geometry and connectivity -> slot s (thread 0 only). With `leave_out` (the
+  // test-only fault mode) the slot's barrier is armed but the copies are not issued, so that
+  // phase never completes and the bounded waits on it run out.
+  auto issue_main = [=](int64_t t, int s, bool leave_out = false) {
     const int64_t e0 = t * EPB;
     mbar_expect_tx(&bar[s], L::QBYTES + L::GEOBYTES + L::CONNBYTES);
+    if (leave_out) return;
 #pragma unroll
     for (int m = 0; m < NF; ++m)
       tma_load(slot_q(s) + m * EPB * NP, gq + ((size_t)m * K + e0) * NP, EPB * NP * 4, &bar[s]);
@@ -465,7 +470,7 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
 
   // prologue: flux of the first tile
   if (is_elem && t0 < ntiles) {
-    if (!mbar_wait(&bar[0], 0u)) {
+    if (!mbar_wait(&bar[0], 0u, wlim)) {
       s_fail = 1;
       atomicOr(P.status, 2);
     }
@@ -502,7 +507,7 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
         if (issuer && !*vfail && (tnext < ntiles || stage)) {
           fence_async_smem();  // order the generic-proxy reads before the copies
           if (tnext < ntiles) {
-            issue_main(tnext, s ^ 1);
+            issue_main(tnext, s ^ 1, P.fault == 1 && it == 1);
             if (s) ++iss0;
             else ++iss1;
           }
@@ -596,7 +601,7 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
         }
       }
       if (tnext < ntiles) {
-        if (!mbar_wait(&bar[s ^ 1], (ph >> (s ^ 1)) & 1u)) {
+        if (!mbar_wait(&bar[s ^ 1], (ph >> (s ^ 1)) & 1u, wlim)) {
           s_fail = 1;
           atomicOr(P.status, 2);
         }
@@ -604,7 +609,7 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
         if (!*vfail) flux_tile(tnext, s ^ 1, sX + (s ^ 1) * NCHAIN * NFP);
       }
       if (stage && !*vfail) {
-        if (!mbar_wait(&bar[2], (ph >> 2) & 1u)) {
+        if (!mbar_wait(&bar[2], (ph >> 2) & 1u, wlim)) {
           s_fail = 1;
           atomicOr(P.status, 2);
         }
@@ -763,9 +768,9 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
   if (issuer) {
     // let the copies this thread issued land before the block exits: immediate when the
     // element threads consumed them, bounded otherwise
-    if (iss0) mbar_wait(&bar[0], (iss0 - 1u) & 1u);
-    if (iss1) mbar_wait(&bar[1], (iss1 - 1u) & 1u);
-    if (iss2) mbar_wait(&bar[2], (iss2 - 1u) & 1u);
+    if (iss0) mbar_wait(&bar[0], (iss0 - 1u) & 1u, wlim);
+    if (iss1) mbar_wait(&bar[1], (iss1 - 1u) & 1u, wlim);
+    if (iss2) mbar_wait(&bar[2], (iss2 - 1u) & 1u, wlim);
   }
 }
 
@@ -856,6 +861,8 @@ int launch_fast_t(const FastLaunch& fl, const FastStageParams& P0, cudaStream_t 
   static const VolGroups vg = volume_groups<N, PHYS, TPE>();
   FastStageParams P = P0;
   for (int g = 0; g < 16; ++g) P.vstart[g] = vg.start[g], P.vlen[g] = vg.len[g];
+  P.wait_iters = fl.wait_iters;
+  P.fault = fl.fault;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES) !=
       cudaSuccess)
     return BB_ERR_CUDA;

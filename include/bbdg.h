@@ -134,6 +134,11 @@ int bb_rhs(bb_solver* s, const void* q, void* rhs, void* stream);
 int bb_lsrk_run(bb_solver* s, double dt, int nsteps, void* q, void* res, int use_graph,
                 void* stream);
 
+/* Reads and clears the solver's device status word (synchronises the stream): BB_OK, or
+ * BB_ERR_TIMEOUT when a bounded device-side wait of its kernels ran out, BB_ERR_DEVICE when
+ * a kernel found corrupt connectivity. bb_rhs checks it itself; bb_lsrk_run does not wait. */
+int bb_solver_check(bb_solver* s, void* stream);
+
 /* The same with host state: copies q_host_in to q_dev, advances, copies back to
  * q_host_out (pinned host memory recommended). */
 int bb_lsrk_run_host(bb_solver* s, double dt, int nsteps, const void* q_host_in,
@@ -243,6 +248,23 @@ int bb_gemm_bf16(bb_ctx* ctx, int64_t M, int N, int K, const void* A, const void
 /* Reads and clears the context's device status word (synchronises the stream); *out = 0 when
  * no kernel reported a problem, bit 0 = a corrupt connectivity entry, bit 1 = a wait ran out. */
 int bb_device_status(bb_ctx* ctx, void* stream, int* out);
+
+/* ---- bounded device-side waits ------------------------------------------------------
+ * No counterpart in the reference (its loops run on the CPU). The bulk-copy pipelines of the
+ * degree-specialised stage kernels, the FP32 lift and the tensor-core GEMM wait on mbarriers;
+ * every such wait gives up after a bounded number of polls, sets a status bit, lets the
+ * kernel's own copies in flight land (bounded) and returns, so the context stays usable. */
+
+/* Polls before a device-side wait gives up, for kernels launched afterwards on this context
+ * (captured solver and batch graphs are rebuilt); 0 = the default, 2^24 polls (about a
+ * second). */
+int bb_ctx_set_wait_limit(bb_ctx* ctx, uint32_t polls);
+/* Test only: mode 1 makes the stage kernels' and the GEMM's copy issuers arm the barrier of
+ * one bulk copy (the stage kernel: the copy issued during each block's second tile; the GEMM:
+ * the second operand stage) without issuing it, so that the bounded wait on it runs out and
+ * the time-out path can be checked; 0 = off (the default). Applies to launches made
+ * afterwards. */
+int bb_ctx_set_test_fault(bb_ctx* ctx, int mode);
 
 /* out[c][r] = in[r][c] for a BF16 [rows x cols] matrix. */
 int bb_transpose_bf16(bb_ctx* ctx, int64_t rows, int cols, const void* in, void* out,
