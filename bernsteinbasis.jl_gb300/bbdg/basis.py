@@ -97,3 +97,46 @@ def gaussian_pulses(seed: int, count: int = 8):
             acc += a * np.exp(-((x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2) / w ** 2)
         return acc
     return f
+
+
+def evaluate_at_points(mesh: TetMesh, N: int, q: np.ndarray, pts: np.ndarray,
+                       chunk: int = 16384) -> np.ndarray:
+    """Values (nf, P) of the degree-N Bernstein fields q (nf, K, Np) of a uniform_tet_mesh at
+    points pts (P, 3) in [-1, 1]^3 (host, FP64). Each point is located in its hexahedron
+    (periodic wrap) and in the one of the hexahedron's six tetrahedra where its barycentric
+    coordinates are all >= 0 (the largest minimum, for points on shared faces)."""
+    if mesh.n < 1 or mesh.K != 6 * mesh.n ** 3:
+        raise ValueError("point location needs a uniform_tet_mesh")
+    q = np.asarray(q, dtype=np.float64)
+    n, h = mesh.n, mesh.h
+    X1 = mesh.EVX[:, 0, :]
+    G = np.stack([mesh.EVX[:, m, :] - X1 for m in (1, 2, 3)], axis=2)   # (K, 3, 3)
+    Ginv = np.linalg.inv(G)
+    lut = np.array(linear_to_ijkl_lookup(N))                           # (Np, 4): i, j, k, l
+    coef = np.array([factorial(N) / (factorial(i) * factorial(j) * factorial(k) * factorial(l))
+                     for (i, j, k, l) in lut])
+    out = np.empty((q.shape[0], pts.shape[0]))
+    for p0 in range(0, pts.shape[0], chunk):
+        P = np.asarray(pts[p0:p0 + chunk], dtype=np.float64)
+        cell = np.clip(np.floor((P + 1.0) / h).astype(np.int64), 0, n - 1)
+        hexid = cell[:, 0] + n * (cell[:, 1] + n * cell[:, 2])
+        best_e = np.zeros(P.shape[0], np.int64)
+        best_l = np.zeros((P.shape[0], 4))
+        best_m = np.full(P.shape[0], -np.inf)
+        for t in range(6):
+            e = 6 * hexid + t
+            # vertex X1 of the element may sit in a neighbouring cell of the unwrapped lattice
+            lam3 = np.einsum("pij,pj->pi", Ginv[e], P - X1[e])             # weights on X2..X4
+            lam = np.concatenate([1.0 - lam3.sum(axis=1, keepdims=True), lam3], axis=1)
+            m = lam.min(axis=1)
+            better = m > best_m
+            best_m = np.where(better, m, best_m)
+            best_e = np.where(better, e, best_e)
+            best_l = np.where(better[:, None], lam, best_l)
+        # coefficient (i, j, k, l) carries lambda_X2^i lambda_X3^j lambda_X4^k lambda_X1^l
+        L1, L2, L3, L4 = (best_l[:, c] for c in range(4))                 # X1, X2, X3, X4
+        B = coef[None, :] * (L2[:, None] ** lut[:, 0] * L3[:, None] ** lut[:, 1] *
+                             L4[:, None] ** lut[:, 2] * L1[:, None] ** lut[:, 3])
+        for f in range(q.shape[0]):
+            out[f, p0:p0 + chunk] = np.einsum("pn,pn->p", B, q[f][best_e])
+    return out

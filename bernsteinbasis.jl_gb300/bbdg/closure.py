@@ -134,10 +134,11 @@ class Closure:
 
     def run_lo(self, q: torch.Tensor, nmacro: int, closure: bool,
                weight: float | None = None) -> None:
+        w = self.weight if weight is None else weight
         for _ in range(nmacro):
             self.plain_macro(q)
-            if closure:
-                self.correct(q, weight)
+            if closure and w != 0.0:
+                self.correct(q, w)
 
     # ---- data ----------------------------------------------------------------------------
     def snapshots(self, seed: int, nmacro: int, rollout: bool = False, noise: float = 0.0):
@@ -186,16 +187,17 @@ class Closure:
 
     def train(self, seeds, nmacro: int, epochs: int = 20, lr: float = 1e-3,
               lr_final: float = 1e-5, rollout_epochs: int = 0, noise: float = 0.0,
-              store_limit_bytes: float = 40e9, log=None) -> dict:
+              store_limit_bytes: float = 40e9, log=None, keep_every: int = 1) -> dict:
         """Teacher-forced phase: generates the snapshot pairs of every seed (kept on the GPU
         up to the store limit) and runs `epochs` passes of Adam over them in shuffled order,
         one snapshot per step. Rollout phase (rollout_epochs > 0): adds the pairs of the
         current network's own corrected trajectories and trains `rollout_epochs` more passes
-        over both sets."""
+        over both sets. keep_every > 1 keeps every keep_every-th snapshot pair of each
+        trajectory (more initial conditions in the same device store)."""
         t0 = time.perf_counter()
         per = self.K * (self.nin * 2 + self.nout * 4)
         cap = max(1, int(store_limit_bytes // per))
-        store = self._generate(seeds, nmacro, False, cap, noise)
+        store = self._generate(seeds, nmacro, False, cap, noise, keep_every)
         torch.cuda.synchronize()
         info = {"snapshots": len(store), "generate_s": time.perf_counter() - t0}
         losses = self._fit(store, epochs, lr, lr_final, log)
@@ -203,18 +205,18 @@ class Closure:
                      "epoch_loss": losses})
         if rollout_epochs > 0:
             t1 = time.perf_counter()
-            store += self._generate(seeds, nmacro, True, cap)
+            store += self._generate(seeds, nmacro, True, cap, 0.0, keep_every)
             losses2 = self._fit(store, rollout_epochs, lr / 10, lr_final, log)
             torch.cuda.synchronize()
             info.update({"rollout_snapshots": len(store), "rollout_s": time.perf_counter() - t1,
                          "rollout_epoch_loss": losses2})
         return info
 
-    def _generate(self, seeds, nmacro, rollout, cap, noise=0.0):
+    def _generate(self, seeds, nmacro, rollout, cap, noise=0.0, keep_every=1):
         store = []
         for s in seeds:
-            for X, T in self.snapshots(s, nmacro, rollout, noise):
-                if len(store) < cap:
+            for j, (X, T) in enumerate(self.snapshots(s, nmacro, rollout, noise)):
+                if len(store) < cap and j % max(1, keep_every) == keep_every // 2:
                     store.append((X, T))
         return store
 
@@ -241,27 +243,34 @@ class Closure:
         return losses
 
     # ---- evaluation ----------------------------------------------------------------------
-    def select_weight(self, seed: int, nmacro: int, weights=(1.0, 0.5, 0.25)) -> dict:
-        """Model selection on a training initial condition: the correction weight whose
-        corrected run ends closest to the (FP32) degree-10 run; sets self.weight."""
+    def select_weight(self, seeds, nmacro: int,
+                      weights=(1.0, 0.75, 0.5, 0.35, 0.25, 0.15, 0.1)) -> dict:
+        """Model selection on validation initial conditions (seeds: one or several, not used
+        for training): the correction weight whose free-running corrected runs end closest,
+        summed over the seeds, to the (FP32) degree-10 runs; sets self.weight. Weight 0 (the
+        plain solver) competes too: when no weight beats it, the closure is switched off
+        rather than shipped with a loss."""
+        seeds = [seeds] if isinstance(seeds, int) else list(seeds)
         hi = self.hi_solver()
-        q = self.initial_state(seed)
-        c0 = project(q, self.cfg.N_hi, self.cfg.N_lo)
-        res = torch.zeros_like(q)
-        hi.run(q, res, self.dt_hi, self.cfg.hi_steps * nmacro)
-        ref = project(q, self.cfg.N_hi, self.cfg.N_lo)
-        errs = {}
-        q5 = c0.clone()
-        self.run_lo(q5, nmacro, False)
-        errs["plain"] = self.rel_l2(q5, ref)
-        for w in weights:
+        errs = {"plain": 0.0, **{f"w{w:g}": 0.0 for w in weights}}
+        for seed in seeds:
+            q = self.initial_state(seed)
+            c0 = project(q, self.cfg.N_hi, self.cfg.N_lo)
+            res = torch.zeros_like(q)
+            hi.run(q, res, self.dt_hi, self.cfg.hi_steps * nmacro)
+            ref = project(q, self.cfg.N_hi, self.cfg.N_lo)
             q5 = c0.clone()
-            self.run_lo(q5, nmacro, True, float(w))
-            e = self.rel_l2(q5, ref)
-            errs[f"w{w:g}"] = e if math.isfinite(e) else float("inf")
+            self.run_lo(q5, nmacro, False)
+            errs["plain"] += self.rel_l2(q5, ref)
+            for w in weights:
+                q5 = c0.clone()
+                self.run_lo(q5, nmacro, True, float(w))
+                e = self.rel_l2(q5, ref)
+                errs[f"w{w:g}"] += e if math.isfinite(e) else float("inf")
         best = min(weights, key=lambda w: errs[f"w{w:g}"])
-        self.weight = float(best)
-        return {"selected_weight": self.weight, "selection_errors": errs}
+        self.weight = float(best) if errs[f"w{best:g}"] < errs["plain"] else 0.0
+        return {"selected_weight": self.weight, "selection_seeds": seeds,
+                "selection_errors_summed": errs}
 
     def apriori(self, seed: int, nmacro: int) -> dict:
         """Teacher-forced one-macro-step error on one trajectory: sum over snapshots of
@@ -330,6 +339,45 @@ class Closure:
             out[f"{name}_lo_finite"] = bool(torch.isfinite(q5).all())
         out["closure_gain"] = out["err_plain_lo"] / max(out["err_closure_lo"], 1e-300)
         out["speedup_closure_vs_hi"] = t_hi / max(out["closure_lo_seconds"], 1e-12)
+        return out
+
+    def truth_errors(self, seed: int, nmacro: int, npoints: int = 200_000,
+                     point_seed: int = 7) -> dict:
+        """Errors against an independent truth: the degree-N_hi FP32 run on the mesh refined
+        twice in each direction (8 times the elements, half the time step), over the same
+        time. The plain degree-N_hi, plain degree-N_lo and closure degree-N_lo runs on this
+        mesh and the truth are evaluated at npoints uniform random points of the cube;
+        relative L2 = RMS of the difference / RMS of the truth (all fields together). The
+        uniform points make the RMS a Monte-Carlo estimate of the L2 norm over the cube."""
+        from .basis import evaluate_at_points
+        from .mesh import uniform_tet_mesh
+        if self.mesh.n < 1:
+            raise ValueError("truth_errors needs a uniform_tet_mesh")
+        N_hi, N_lo = self.cfg.N_hi, self.cfg.N_lo
+        fine = uniform_tet_mesh(2 * self.mesh.n)
+        sf = DGSolver(fine, N_hi, "maxwell", torch.float32, self.cfg.tau, self.device)
+        autotune.tune(sf)
+        qf = sf.project(maxwell_ic(seed, self.cfg.pulses))
+        rf = torch.zeros_like(qf)
+        sf.run(qf, rf, self.dt_hi / 2, 2 * self.cfg.hi_steps * nmacro)
+        pts = np.random.default_rng(point_seed).uniform(-1.0, 1.0, (npoints, 3))
+        truth = evaluate_at_points(fine, N_hi, qf.double().cpu().numpy(), pts)
+        del qf, rf, sf
+        hi = self.hi_solver()
+        q = self.initial_state(seed)
+        c0 = project(q, N_hi, N_lo)
+        res = torch.zeros_like(q)
+        hi.run(q, res, self.dt_hi, self.cfg.hi_steps * nmacro)
+        vals = {"hi": evaluate_at_points(self.mesh, N_hi, q.double().cpu().numpy(), pts)}
+        for name, cl in (("plain_lo", False), ("closure_lo", True)):
+            q5 = c0.clone()
+            self.run_lo(q5, nmacro, cl)
+            vals[name] = evaluate_at_points(self.mesh, N_lo, q5.double().cpu().numpy(), pts)
+        scale = math.sqrt(float(np.mean(truth ** 2)))
+        out = {"seed": seed, "t_final": nmacro * self.macro, "truth": f"degree {N_hi} FP32 on "
+               f"{2 * self.mesh.n}^3 x 6 elements", "points": npoints, "weight": self.weight}
+        for k, v in vals.items():
+            out[f"truth_err_{k}"] = math.sqrt(float(np.mean((v - truth) ** 2))) / scale
         return out
 
     def solve(self, seed: int, nmacro: int, growth_tol: float = 1e-2):

@@ -191,9 +191,13 @@ def config4(steps: int = 100, dtype=torch.float32, compare_single: bool = True):
 def config5(n: int = 16, n_train: int = 16, nmacro_train: int = 40, epochs: int = 20,
             n_eval: int = 2, nmacro_eval: int = 40, seed: int = 3, lr: float = 1e-3,
             hidden=(512, 512), N_hi: int = 10, N_lo: int = 5, rollout_epochs: int = 0,
-            noise: float = 0.0, store_gb: float = 40.0):
+            noise: float = 0.0, store_gb: float = 40.0, keep_every: int = 1,
+            fp64_ref_seeds: int = 2, truth_seeds: int = 0, truth_points: int = 200_000):
     """Closure training and held-out evaluation. Training initial conditions are drawn from
-    `seed`, the held-out ones from seed + 1000; every number is measured on the GPU."""
+    `seed`, the held-out ones from seed + 1000; every number is measured on the GPU. The
+    first fp64_ref_seeds held-out seeds are scored against the FP64 degree-N_hi run, the rest
+    against the FP32 one (the two differ by rounding, about 1e-6, far below the degree-N_lo
+    errors); the first truth_seeds are also scored against the refined-mesh truth."""
     from .closure import Closure, ClosureConfig
     mesh = uniform_tet_mesh(n)
     cl = Closure(mesh, ClosureConfig(N_hi=N_hi, N_lo=N_lo, hidden=tuple(hidden)), seed=seed)
@@ -206,29 +210,38 @@ def config5(n: int = 16, n_train: int = 16, nmacro_train: int = 40, epochs: int 
             "nmacro_train": nmacro_train, "t_train": nmacro_train * cl.macro, "epochs": epochs,
             "n_eval": n_eval, "nmacro_eval": nmacro_eval, "t_eval": nmacro_eval * cl.macro,
             "mlp": list(cl.net.dims), "params": cl.net.num_params,
-            "rollout_epochs": rollout_epochs, "noise": noise}
+            "rollout_epochs": rollout_epochs, "noise": noise, "keep_every": keep_every,
+            "fp64_ref_seeds": fp64_ref_seeds, "truth_seeds": truth_seeds}
     print(json.dumps(head), flush=True)
     cl.fit_scales(train_seeds[0], 3)
     info = cl.train(train_seeds, nmacro_train, epochs=epochs, lr=lr, lr_final=lr / 100,
                     rollout_epochs=rollout_epochs, noise=noise,
                     store_limit_bytes=store_gb * 1e9,
-                    log=lambda s: print(s, flush=True))
+                    log=lambda s: print(s, flush=True), keep_every=keep_every)
     info.update({"s_in": cl.s_in, "s_out": cl.s_out})
     print(json.dumps({"train": info}), flush=True)
-    sel = cl.select_weight(train_seeds[0], nmacro_eval)
+    val_seeds = [int(s) for s in np.random.default_rng(seed + 500).integers(0, 2**31 - 1, 2)]
+    sel = cl.select_weight(val_seeds, nmacro_eval)
     print(json.dumps({"model_selection": sel}), flush=True)
     rows = []
-    for s in eval_seeds:
-        r = cl.evaluate(s, nmacro_eval, weights=(1.0, 0.5, 0.25))
+    for i, s in enumerate(eval_seeds):
+        ref = torch.float64 if i < fp64_ref_seeds else torch.float32
+        r = cl.evaluate(s, nmacro_eval, reference_dtype=ref, weights=(1.0, 0.5, 0.25))
         r["weight"] = cl.weight
+        r["reference"] = "fp64" if ref == torch.float64 else "fp32"
         r.update(cl.apriori(s, nmacro_eval))
+        if i < truth_seeds:
+            r.update(cl.truth_errors(s, nmacro_eval, npoints=truth_points))
         rows.append(r)
         print(json.dumps(r), flush=True)
     summ = {"config": 5, "summary": True,
             "err_plain_lo_mean": float(np.mean([r["err_plain_lo"] for r in rows])),
             "err_closure_lo_mean": float(np.mean([r["err_closure_lo"] for r in rows])),
-            "err_hi_vs_fp64_hi_mean": float(np.mean([r["err_hi_vs_fp64_hi"] for r in rows])),
+            "err_hi_vs_fp64_hi_mean": float(np.mean([r["err_hi_vs_fp64_hi"] for r in rows
+                                                     if r["reference"] == "fp64"] or [np.nan])),
             "closure_gain_mean": float(np.mean([r["closure_gain"] for r in rows])),
+            "closure_gain_min": float(np.min([r["closure_gain"] for r in rows])),
+            "weight": cl.weight,
             "apriori_gain_mean": float(np.mean([r["apriori_gain"] for r in rows])),
             "speedup_closure_vs_hi_mean": float(np.mean([r["speedup_closure_vs_hi"]
                                                          for r in rows]))}
@@ -251,6 +264,12 @@ def main():
     ap.add_argument("--N-lo", type=int, default=5)
     ap.add_argument("--rollout-epochs", type=int, default=0)
     ap.add_argument("--noise", type=float, default=0.0)
+    ap.add_argument("--keep-every", type=int, default=1,
+                    help="config 5: keep every k-th snapshot pair of a training trajectory")
+    ap.add_argument("--fp64-ref-seeds", type=int, default=2)
+    ap.add_argument("--truth-seeds", type=int, default=0,
+                    help="config 5: held-out seeds also scored against the refined-mesh truth")
+    ap.add_argument("--truth-points", type=int, default=200_000)
     ap.add_argument("--store-gb", type=float, default=40.0,
                     help="device memory for the training snapshot store (per phase)")
     ap.add_argument("--steps", type=int, default=None)
@@ -272,7 +291,9 @@ def main():
         config5(n=a.n, n_train=a.n_train, nmacro_train=a.nmacro_train, epochs=a.epochs,
                 n_eval=a.n_eval, nmacro_eval=a.nmacro_eval, lr=a.lr,
                 hidden=tuple(int(v) for v in a.hidden.split(",")), N_hi=a.N_hi, N_lo=a.N_lo,
-                rollout_epochs=a.rollout_epochs, noise=a.noise, store_gb=a.store_gb)
+                rollout_epochs=a.rollout_epochs, noise=a.noise, store_gb=a.store_gb,
+                keep_every=a.keep_every, fp64_ref_seeds=a.fp64_ref_seeds,
+                truth_seeds=a.truth_seeds, truth_points=a.truth_points)
 
 
 if __name__ == "__main__":

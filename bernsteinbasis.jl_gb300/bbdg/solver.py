@@ -167,6 +167,40 @@ class DGSolver:
         """0.5 * integral of the squared fields (the wave / Maxwell energy)."""
         return 0.5 * float(self.mass_norms(q).sum())
 
+    # ---- checkpoints ---------------------------------------------------------------------
+    def mesh_fingerprint(self) -> str:
+        """Hash of the connectivity and geometry records: a checkpoint fits this mesh only."""
+        import hashlib
+        h = hashlib.sha1()
+        h.update(np.ascontiguousarray(self.mesh.conn, dtype=np.int32).tobytes())
+        h.update(np.ascontiguousarray(self.mesh.geo, dtype=np.float64).tobytes())
+        return h.hexdigest()[:20]
+
+    def save_state(self, path: str, q: torch.Tensor, res: torch.Tensor, t: float = 0.0,
+                   step: int = 0, as_fp64: bool = False) -> None:
+        """Writes q, the LSRK register res, the time and the step count to an .npz file,
+        in the solver's dtype or (as_fp64) widened to FP64, so that a run can resume, or an
+        FP64 state can seed FP32 checks from the same point."""
+        self._check_state(q, res)
+        cast = (lambda x: x.double()) if as_fp64 else (lambda x: x)
+        np.savez(path, q=cast(q).cpu().numpy(), res=cast(res).cpu().numpy(), t=float(t),
+                 step=int(step), N=self.N, physics=self.physics, tau=self.tau,
+                 mesh=self.mesh_fingerprint(), dtype=str(self.dtype))
+
+    def load_state(self, path: str):
+        """Reads a checkpoint of save_state into new device tensors of this solver's dtype.
+        Returns (q, res, t, step). Raises ValueError if it was written for another degree,
+        physics, penalty or mesh."""
+        z = np.load(path if path.endswith(".npz") else path + ".npz")
+        want = (self.N, self.physics, self.tau, self.mesh_fingerprint())
+        got = (int(z["N"]), str(z["physics"]), float(z["tau"]), str(z["mesh"]))
+        if got != want:
+            raise ValueError(f"checkpoint {got} does not match this solver {want}")
+        q = torch.as_tensor(z["q"]).to(device=self.device, dtype=self.dtype).contiguous()
+        res = torch.as_tensor(z["res"]).to(device=self.device, dtype=self.dtype).contiguous()
+        self._check_state(q, res)
+        return q, res, float(z["t"]), int(z["step"])
+
     def close(self) -> None:
         if getattr(self, "handle", None):
             _lib.load().bb_solver_destroy(self.handle)

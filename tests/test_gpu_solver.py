@@ -358,3 +358,31 @@ def test_external_integrator_drives_the_rhs(cuda, bb, oracle_cpu):
     want = rk4(lambda t, q: oracle_cpu.rhs(0, N, q, md, tau=1.0), np.asarray(q0))
     err = per_field_rel(got, want)
     assert np.all(err < 1e-12), err
+
+
+def test_checkpoint_resume_is_bitwise_and_fp64_dump_seeds_fp32(cuda, bb, tmp_path):
+    """save_state / load_state: 3 steps, checkpoint, 4 more steps equals 7 steps in one go
+    (bitwise); an FP64 checkpoint loads into an FP32 solver as the rounded state; a
+    checkpoint of another degree or mesh is refused."""
+    import torch
+    m = bb.uniform_tet_mesh(3)
+    s = bb.DGSolver(m, 4, "maxwell", dtype=torch.float32, tau=1.0)
+    q0 = s.project([bb.gaussian_pulses(f + 1) for f in range(6)])
+    dt = s.dt_cfl()
+    qa, ra = q0.clone(), torch.zeros_like(q0)
+    s.run(qa, ra, dt, 7)
+    qb, rb = q0.clone(), torch.zeros_like(q0)
+    s.run(qb, rb, dt, 3)
+    s.save_state(str(tmp_path / "ck"), qb, rb, t=3 * dt, step=3)
+    qc, rc, t, step = s.load_state(str(tmp_path / "ck.npz"))
+    assert step == 3 and t == 3 * dt
+    s.run(qc, rc, dt, 4)
+    assert torch.equal(qc, qa) and torch.equal(rc, ra)
+    s64 = bb.DGSolver(m, 4, "maxwell", dtype=torch.float64, tau=1.0)
+    q64 = s64.project([bb.gaussian_pulses(f + 1) for f in range(6)])
+    s64.save_state(str(tmp_path / "ck64"), q64, torch.zeros_like(q64), as_fp64=True)
+    q32, _, _, _ = s.load_state(str(tmp_path / "ck64.npz"))
+    assert torch.equal(q32, q64.float())
+    other = bb.DGSolver(m, 5, "maxwell", dtype=torch.float32, tau=1.0)
+    with pytest.raises(ValueError):
+        other.load_state(str(tmp_path / "ck.npz"))
