@@ -13,7 +13,7 @@ from . import _build
 BB_OK, BB_ERR_ARG, BB_ERR_CUDA, BB_ERR_TIMEOUT, BB_ERR_NONFINITE, BB_ERR_STATE, \
     BB_ERR_NOMEM, BB_ERR_DEVICE = range(8)
 BB_F32, BB_F64 = 0, 1
-BB_WAVE, BB_MAXWELL, BB_ADVECTION = 0, 1, 2
+BB_WAVE, BB_MAXWELL, BB_ADVECTION, BB_ADVECTION3 = 0, 1, 2, 3
 GEO_STRIDE = 24
 
 _STATUS_NAMES = {0: "BB_OK", 1: "BB_ERR_ARG", 2: "BB_ERR_CUDA", 3: "BB_ERR_TIMEOUT",

@@ -23,7 +23,7 @@ from .mesh import TetMesh
 from .ordering import np3
 
 PHYSICS = {"wave": (_lib.BB_WAVE, 4), "maxwell": (_lib.BB_MAXWELL, 6),
-           "advection": (_lib.BB_ADVECTION, 1)}
+           "advection": (_lib.BB_ADVECTION, 1), "advection3": (_lib.BB_ADVECTION3, 3)}
 
 
 class DGSolver:

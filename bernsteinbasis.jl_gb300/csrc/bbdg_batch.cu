@@ -392,7 +392,7 @@ extern "C" int bb_batch_create(bb_ctx* ctx, int nprob, const bb_batch_problem* p
   b->dtype = dtype;
   for (int p = 0; p < nprob; ++p) {
     const bb_batch_problem& pr = probs[p];
-    if (physics_nf(pr.physics) == 0 || !valid_degree(pr.N) || pr.K < 1 ||
+    if (physics_nf(pr.physics) == 0 || pr.physics == BB_ADVECTION3 || !valid_degree(pr.N) || pr.K < 1 ||
         pr.K >= (int64_t(1) << 27) || !pr.conn || !pr.geo || !pr.q || !pr.res ||
         !std::isfinite(pr.dt) || !std::isfinite(pr.tau)) {
       free_batch(b);

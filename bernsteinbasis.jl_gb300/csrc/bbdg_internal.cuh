@@ -143,7 +143,12 @@ int bb_device_status_error(bb_ctx* ctx, int word);
 inline size_t dtype_size(int dtype) { return dtype == BB_F64 ? 8 : 4; }
 // Fields of a physics code, 0 if unknown.
 __host__ __device__ inline int physics_nf(int physics) {
-  return physics == BB_WAVE ? 4 : physics == BB_MAXWELL ? 6 : physics == BB_ADVECTION ? 1 : 0;
+  return physics == BB_WAVE ? 4 : physics == BB_MAXWELL ? 6 : physics == BB_ADVECTION ? 1
+       : physics == BB_ADVECTION3 ? 3 : 0;
+}
+// Volume-term components of a physics (the advection examples have one: J du/dx).
+__host__ __device__ inline int physics_nw(int physics) {
+  return physics == BB_ADVECTION3 ? 1 : physics_nf(physics);
 }
 inline bool valid_dtype(int dtype) { return dtype == BB_F32 || dtype == BB_F64; }
 inline bool valid_degree(int N) { return N >= 1 && N <= BB_MAX_DEGREE; }

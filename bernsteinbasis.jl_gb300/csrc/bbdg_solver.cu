@@ -91,6 +91,9 @@ int solver_layout(bb_solver* s, int epb, size_t* smem_out, int* chain_out = null
   else if (s->physics == BB_ADVECTION)
     L = s->dtype == BB_F64 ? tile_layout<double, BB_ADVECTION>(*s->tab, epb)
                            : tile_layout<float, BB_ADVECTION>(*s->tab, epb);
+  else if (s->physics == BB_ADVECTION3)
+    L = s->dtype == BB_F64 ? tile_layout<double, BB_ADVECTION3>(*s->tab, epb)
+                           : tile_layout<float, BB_ADVECTION3>(*s->tab, epb);
   else
     L = s->dtype == BB_F64 ? tile_layout<double, BB_MAXWELL>(*s->tab, epb)
                            : tile_layout<float, BB_MAXWELL>(*s->tab, epb);
@@ -187,6 +190,10 @@ int launch_stage(bb_solver* s, int mode, int stage, double dt, void* q, void* re
     return s->dtype == BB_F64
                ? launch_stage_t<double, BB_ADVECTION>(s, mode, stage, dt, q, res, rhs, tin, tout, st)
                : launch_stage_t<float, BB_ADVECTION>(s, mode, stage, dt, q, res, rhs, tin, tout, st);
+  if (s->physics == BB_ADVECTION3)
+    return s->dtype == BB_F64
+               ? launch_stage_t<double, BB_ADVECTION3>(s, mode, stage, dt, q, res, rhs, tin, tout, st)
+               : launch_stage_t<float, BB_ADVECTION3>(s, mode, stage, dt, q, res, rhs, tin, tout, st);
   return s->dtype == BB_F64
              ? launch_stage_t<double, BB_MAXWELL>(s, mode, stage, dt, q, res, rhs, tin, tout, st)
              : launch_stage_t<float, BB_MAXWELL>(s, mode, stage, dt, q, res, rhs, tin, tout, st);
@@ -203,6 +210,8 @@ int launch_extract(bb_solver* s, const void* q, void* tr, cudaStream_t st) {
       extract_traces_kernel<double, 4><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr);
     else if (s->nf == 1)
       extract_traces_kernel<double, 1><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr);
+    else if (s->nf == 3)
+      extract_traces_kernel<double, 3><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr);
     else
       extract_traces_kernel<double, 6><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr);
   } else {
@@ -210,6 +219,8 @@ int launch_extract(bb_solver* s, const void* q, void* tr, cudaStream_t st) {
       extract_traces_kernel<float, 4><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr);
     else if (s->nf == 1)
       extract_traces_kernel<float, 1><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr);
+    else if (s->nf == 3)
+      extract_traces_kernel<float, 3><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr);
     else
       extract_traces_kernel<float, 6><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr);
   }
@@ -270,7 +281,8 @@ extern "C" int bb_solver_create(bb_ctx* ctx, int physics, int N, int64_t K, int 
   if (!ctx || !out) return BB_ERR_ARG;
   *out = nullptr;
   if (physics_nf(physics) == 0)
-    return bb_fail(ctx, BB_ERR_ARG, "physics must be BB_WAVE, BB_MAXWELL or BB_ADVECTION");
+    return bb_fail(ctx, BB_ERR_ARG,
+                   "physics must be BB_WAVE, BB_MAXWELL, BB_ADVECTION or BB_ADVECTION3");
   if (!valid_degree(N)) return bb_fail(ctx, BB_ERR_ARG, "degree N=%d outside 1..%d", N, BB_MAX_DEGREE);
   if (!valid_dtype(dtype)) return bb_fail(ctx, BB_ERR_ARG, "bad dtype");
   if (K < 1 || K >= (int64_t(1) << 27)) return bb_fail(ctx, BB_ERR_ARG, "K must be in 1..2^27-1");
@@ -407,7 +419,7 @@ extern "C" int bb_stage_tile_bytes(int physics, int N, int dtype, int epb, int64
     return BB_ERR_ARG;
   const int nwords = deg_table_words(N);
   const int nf = physics_nf(physics);
-  const TileLayout L = tile_layout_for(N, nf, nf, dtype_size(dtype), nwords, epb);
+  const TileLayout L = tile_layout_for(N, nf, physics_nw(physics), dtype_size(dtype), nwords, epb);
   *bytes = (int64_t)L.total;
   if (chain) *chain = L.chain;
   return BB_OK;

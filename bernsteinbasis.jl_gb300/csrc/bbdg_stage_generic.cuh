@@ -43,6 +43,15 @@ struct Phys<BB_ADVECTION> {
   static constexpr int NCH = 1;
   static constexpr float vol_sign = -1.f;
 };
+// examples/3d_advec.jl: q = (u, v, w), fx(q) = (u, 0, 0), fy = fz = 0: the flux of the
+// scalar example on each component, the volume term on u only; du = -(...) / J as above.
+template <>
+struct Phys<BB_ADVECTION3> {
+  static constexpr int NF = 3;  // u, v, w
+  static constexpr int NW = 1;  // J du/dx (v and w have no volume term)
+  static constexpr int NCH = 3;
+  static constexpr float vol_sign = -1.f;
+};
 
 template <class T>
 struct StageParams {
@@ -253,10 +262,12 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
       const T nx = g[12 + f], ny = g[16 + f], nz = g[20 + f];
       const T cp = sPen[(le * 4 + f) * 2], cu = sPen[(le * 4 + f) * 2 + 1];
       T fl[NF];
-      if constexpr (PHYS == BB_ADVECTION) {
-        // 3d_advec_scalar.jl:24-29: 0.5 du nxJ - 0.5 du Jf (negated, see Phys<BB_ADVECTION>)
+      if constexpr (PHYS == BB_ADVECTION || PHYS == BB_ADVECTION3) {
+        // 3d_advec_scalar.jl:24-29, 3d_advec.jl:44-45: 0.5 du nxJ - 0.5 du Jf per component
+        // (negated, see Phys<BB_ADVECTION>)
         const T Jf = sqrt(nx * nx + ny * ny + nz * nz);
-        fl[0] = -(T(0.5) * d[0] * nx - T(0.5) * d[0] * Jf);
+#pragma unroll
+        for (int m = 0; m < NF; ++m) fl[m] = -(T(0.5) * d[m] * nx - T(0.5) * d[m] * Jf);
       } else if constexpr (PHYS == BB_WAVE) {
         // 3d_wave.jl:45-54
         // the velocity flux 0.5 B (nx, ny, nz) is stored as the scalar 0.5 B; the lift
@@ -304,7 +315,7 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
       for (int m = 0; m < NW; ++m) w[m] = T(0);
       // sum_a g_a x(beta+e_a) with sum_a g_a = 0, formed as sum_{a<3} g_a (x_a - x_3) so
       // that smooth data cancels in the differences (as the reference's Dr = (D0 - D3)/2)
-      if constexpr (PHYS == BB_ADVECTION) {
+      if constexpr (PHYS == BB_ADVECTION || PHYS == BB_ADVECTION3) {
         const T u3 = F(0, 3);
 #pragma unroll
         for (int a = 0; a < 3; ++a) w[0] += gx[a] * (F(0, a) - u3);  // J du/dx
@@ -368,8 +379,10 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
         for (int m = 0; m < NW; ++m) acc[m] += small_int<T>(l) * wb[m * ws + x];
       }
 #pragma unroll
-      for (int m = 0; m < NF; ++m)
-        sOut[((size_t)m * epb + le) * Np + n] = Phys<PHYS>::vol_sign < 0 ? -acc[m] : acc[m];
+      for (int m = 0; m < NF; ++m) {
+        const T v = m < NW ? acc[m < NW ? m : 0] : T(0);  // fields past NW: no volume term
+        sOut[((size_t)m * epb + le) * Np + n] = Phys<PHYS>::vol_sign < 0 ? -v : v;
+      }
     }
     __syncthreads();
 

@@ -42,8 +42,11 @@ typedef enum {
 typedef enum { BB_F32 = 0, BB_F64 = 1 } bb_dtype;
 /* BB_WAVE: examples/3d_wave.jl (p, u, v, w); BB_MAXWELL: examples/3d_maxwell.jl
  * (Hx, Hy, Hz, Ex, Ey, Ez); BB_ADVECTION: examples/3d_advec_scalar.jl (u, du/dt + du/dx = 0,
- * upwind flux with the face Jacobian; tau does not enter, the generic kernel runs it). */
-typedef enum { BB_WAVE = 0, BB_MAXWELL = 1, BB_ADVECTION = 2 } bb_physics;
+ * upwind flux with the face Jacobian; tau does not enter, the generic kernel runs it);
+ * BB_ADVECTION3: examples/3d_advec.jl (u, v, w with fx = (u, 0, 0): the same interface flux
+ * on all three components, the volume term on u only; generic kernel, single solvers only,
+ * not in batches). */
+typedef enum { BB_WAVE = 0, BB_MAXWELL = 1, BB_ADVECTION = 2, BB_ADVECTION3 = 3 } bb_physics;
 typedef enum { BB_AXIS_R = 0, BB_AXIS_S = 1, BB_AXIS_T = 2 } bb_axis;
 
 #define BB_MAX_DEGREE 20

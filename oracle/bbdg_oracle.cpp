@@ -362,13 +362,14 @@ void rhs_example(int N, int K, const SV<T, NF>* q, SV<T, NF>* du, const int* Fma
         cu = tau / Jf;
       }
       V fl;
-      if constexpr (NF == 1) {
-        // examples/3d_advec_scalar.jl:24-29: upwind flux of du/dt + du/dx = 0 with the face
-        // Jacobian Jf = |nJ| (written with Jf as the examples do; tau does not enter)
+      if constexpr (NF == 1 || NF == 3) {
+        // examples/3d_advec_scalar.jl:24-29 and 3d_advec.jl:44-45: upwind flux of
+        // du/dt + du/dx = 0 with the face Jacobian Jf = |nJ| (written with Jf as the examples
+        // do; tau does not enter), on the SVector (u, v, w) in 3d_advec.jl
         const T Jf = std::sqrt(nx * nx + ny * ny + nz * nz);
         (void)cp;
         (void)cu;
-        fl.v[0] = T(0.5) * duM.v[0] * nx - T(0.5) * duM.v[0] * Jf;
+        for (int f = 0; f < NF; ++f) fl.v[f] = T(0.5) * duM.v[f] * nx - T(0.5) * duM.v[f] * Jf;
       } else if constexpr (NF == 4) {
         const T ndotdU = nx * duM.v[1] + ny * duM.v[2] + nz * duM.v[3];
         const T a = cp * duM.v[0] - ndotdU;
@@ -410,6 +411,11 @@ void rhs_example(int N, int K, const SV<T, NF>* q, SV<T, NF>* du, const int* Fma
           fxu[n] = qe[n];  // fx(u) = u, fy = fz = 0 (3d_advec_scalar.jl:33-35)
           fyu[n] = V{};
           fzu[n] = V{};
+        } else if constexpr (NF == 3) {
+          fxu[n] = V{};    // fx(q) = (u, 0, 0), fy = fz = 0 (3d_advec.jl:20-33)
+          fxu[n].v[0] = qe[n].v[0];
+          fyu[n] = V{};
+          fzu[n] = V{};
         } else if constexpr (NF == 4) {
           wave_fluxes(qe[n], fxu[n], fyu[n], fzu[n]);
         } else {
@@ -438,8 +444,8 @@ void rhs_example(int N, int K, const SV<T, NF>* q, SV<T, NF>* du, const int* Fma
         else
           due[i] = due[i] + vol;  // Maxwell: du += ... (3d_maxwell.jl:85); advection :38-40
       }
-      if constexpr (NF == 1)
-        for (int i = 0; i < Np; ++i) due[i] = V::zero() - due[i];  // du = -du / J (:41)
+      if constexpr (NF == 1 || NF == 3)  // du = -du / J (3d_advec_scalar.jl:41, 3d_advec.jl:61)
+        for (int i = 0; i < Np; ++i) due[i] = V::zero() - due[i];
       // du ./= J[1,1]  (3d_wave.jl:83), or the element's own J
       const T Je = Jall ? Jall[e] : J;
       for (int i = 0; i < Np; ++i) due[i] = due[i] / Je;
@@ -543,7 +549,8 @@ void oracle_lift_f32(int N, int K, const float* x, float* out, int nthreads) {
 }
 
 // phys: 0 = wave (4 fields), 1 = Maxwell (6 fields), 2 = scalar advection (1 field,
-// examples/3d_advec_scalar.jl). q/du are AoS Np x K of SVector{nf}.
+// examples/3d_advec_scalar.jl), 3 = three-component advection (3 fields, examples/3d_advec.jl).
+// q/du are AoS Np x K of SVector{nf}.
 int oracle_rhs_f64(int phys, int N, int K, const double* q, double* du, const int* Fmask,
                    const int64_t* mapP, const double* geo9, const double* nJ, double J,
                    const double* Jall, double tau, int nthreads) {
@@ -552,6 +559,9 @@ int oracle_rhs_f64(int phys, int N, int K, const double* q, double* du, const in
                            geo9, nJ, J, Jall, tau, nthreads);
   else if (phys == 2)
     rhs_example<double, 1>(N, K, (const SV<double, 1>*)q, (SV<double, 1>*)du, Fmask, mapP,
+                           geo9, nJ, J, Jall, tau, nthreads);
+  else if (phys == 3)
+    rhs_example<double, 3>(N, K, (const SV<double, 3>*)q, (SV<double, 3>*)du, Fmask, mapP,
                            geo9, nJ, J, Jall, tau, nthreads);
   else if (phys == 1)
     rhs_example<double, 6>(N, K, (const SV<double, 6>*)q, (SV<double, 6>*)du, Fmask, mapP,
@@ -567,6 +577,8 @@ int oracle_rhs_f32(int phys, int N, int K, const float* q, float* du, const int*
     rhs_example<float, 4>(N, K, (const SV<float, 4>*)q, (SV<float, 4>*)du, Fmask, mapP, geo9, nJ, J, Jall, tau, nthreads);
   else if (phys == 2)
     rhs_example<float, 1>(N, K, (const SV<float, 1>*)q, (SV<float, 1>*)du, Fmask, mapP, geo9, nJ, J, Jall, tau, nthreads);
+  else if (phys == 3)
+    rhs_example<float, 3>(N, K, (const SV<float, 3>*)q, (SV<float, 3>*)du, Fmask, mapP, geo9, nJ, J, Jall, tau, nthreads);
   else if (phys == 1)
     rhs_example<float, 6>(N, K, (const SV<float, 6>*)q, (SV<float, 6>*)du, Fmask, mapP, geo9, nJ, J, Jall, tau, nthreads);
   else
@@ -581,6 +593,8 @@ int oracle_lsrk_f64(int phys, int N, int K, double* q, double* res, const int* F
     lsrk_run<double, 4>(N, K, (SV<double, 4>*)q, (SV<double, 4>*)res, Fmask, mapP, geo9, nJ, J, Jall, tau, dt, nsteps, nthreads);
   else if (phys == 2)
     lsrk_run<double, 1>(N, K, (SV<double, 1>*)q, (SV<double, 1>*)res, Fmask, mapP, geo9, nJ, J, Jall, tau, dt, nsteps, nthreads);
+  else if (phys == 3)
+    lsrk_run<double, 3>(N, K, (SV<double, 3>*)q, (SV<double, 3>*)res, Fmask, mapP, geo9, nJ, J, Jall, tau, dt, nsteps, nthreads);
   else if (phys == 1)
     lsrk_run<double, 6>(N, K, (SV<double, 6>*)q, (SV<double, 6>*)res, Fmask, mapP, geo9, nJ, J, Jall, tau, dt, nsteps, nthreads);
   else
@@ -595,6 +609,9 @@ int oracle_lsrk_f32(int phys, int N, int K, float* q, float* res, const int* Fma
                        tau, dt, nsteps, nthreads);
   else if (phys == 2)
     lsrk_run<float, 1>(N, K, (SV<float, 1>*)q, (SV<float, 1>*)res, Fmask, mapP, geo9, nJ, J, Jall,
+                       tau, dt, nsteps, nthreads);
+  else if (phys == 3)
+    lsrk_run<float, 3>(N, K, (SV<float, 3>*)q, (SV<float, 3>*)res, Fmask, mapP, geo9, nJ, J, Jall,
                        tau, dt, nsteps, nthreads);
   else if (phys == 1)
     lsrk_run<float, 6>(N, K, (SV<float, 6>*)q, (SV<float, 6>*)res, Fmask, mapP, geo9, nJ, J, Jall,

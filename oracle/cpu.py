@@ -122,7 +122,8 @@ def _jall(md, dt_, per_element_J):
 def rhs(phys: int, N: int, q_soa: np.ndarray, md, tau: float = 0.0,
         nthreads: int = 0, per_element_J: bool = False) -> np.ndarray:
     """Example right-hand side (wave phys=0, Maxwell phys=1, scalar advection phys=2,
-    examples/3d_advec_scalar.jl) on SoA state (nf, K, Np).
+    examples/3d_advec_scalar.jl, three-component advection phys=3, examples/3d_advec.jl) on
+    SoA state (nf, K, Np).
 
     tau <= 0 evaluates the examples' flux as written; tau > 0 scales the penalty by the
     face Jacobian (upwind penalty tau). per_element_J divides by each element's own J instead

@@ -207,3 +207,41 @@ def test_advection_example_analytic_solution(oracle_cpu, bb):
     u = np.einsum("pn,kn->kp", V, qT[0])
     ex = np.sin(np.pi * (x - T)) * np.sin(np.pi * y) * np.sin(np.pi * z)
     assert np.abs(u - ex).max() < 1e-3
+
+
+def test_three_component_advection_oracle(oracle_cpu, bb):
+    """examples/3d_advec.jl: q = (u, v, w), fx(q) = (u, 0, 0), the scalar example's flux on
+    every component. The u component equals the scalar example bitwise; v and w, which have
+    no volume term, follow the lifted interface flux alone (zero data stays zero); the
+    example's end check (u0 = (sin sin sin, 0, 0), N = 7, 4^3 hexes, T = 0.1) holds."""
+    m = bb.uniform_tet_mesh(3)
+    N = 4
+    md = meshdata.build(m, N)
+    rng = np.random.default_rng(17)
+    q = rng.uniform(-1, 1, (3, m.K, bb.np3(N)))
+    r3 = oracle_cpu.rhs(3, N, q, md)
+    r1 = oracle_cpu.rhs(2, N, q[:1], md)
+    assert np.array_equal(r3[0], r1[0])
+    assert np.abs(r3[1]).max() > 0 and np.abs(r3[2]).max() > 0
+    # v alone, with u = w = 0: only the lifted flux of v acts, linear in v
+    qv = np.zeros_like(q)
+    qv[1] = q[1]
+    rv = oracle_cpu.rhs(3, N, qv, md)
+    assert np.abs(rv[0]).max() == 0 and np.abs(rv[2]).max() == 0
+    np.testing.assert_allclose(oracle_cpu.rhs(3, N, 2 * qv, md)[1], 2 * rv[1], rtol=1e-13,
+                               atol=1e-13)
+    m4 = bb.uniform_tet_mesh(4)
+    N = 7
+    md4 = meshdata.build(m4, N)
+    f0 = lambda x, y, z: np.sin(np.pi * x) * np.sin(np.pi * y) * np.sin(np.pi * z)
+    zero = lambda x, y, z: 0 * x
+    q0 = bb.project_fields(m4, N, [f0, zero, zero])
+    T, nsteps = 0.1, 100
+    qT, _ = oracle_cpu.lsrk(3, N, q0, md4, T / nsteps, nsteps)
+    X = bb.element_domain_points(m4, N)
+    x, y, z = X[..., 0], X[..., 1], X[..., 2]
+    V = bb.bernstein_basis_tet(N, *(2 * bb.mesh.reference_domain_points(N)[:, [1, 2, 3]].T - 1))
+    u = np.einsum("pn,kn->kp", V, qT[0])
+    ex = np.sin(np.pi * (x - T)) * np.sin(np.pi * y) * np.sin(np.pi * z)
+    assert np.abs(u - ex).max() < 1e-3
+    assert np.abs(qT[1:]).max() == 0
