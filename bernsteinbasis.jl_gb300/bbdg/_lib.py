@@ -54,6 +54,8 @@ SIGNATURES = {
     "bb_solver_get_tile": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "bb_solver_set_kernel": (_I, [_P, _I]),
     "bb_solver_get_kernel": (_I, [_P]),
+    "bb_fast_variant": (_I, [_I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
+                             ctypes.POINTER(_I)]),
     "bb_stage_tile_bytes": (_I, [_I, _I, _I, _I, ctypes.POINTER(_I64), ctypes.POINTER(_I)]),
     "bb_rhs": (_I, [_P, _P, _P, _P]),
     "bb_lsrk_run": (_I, [_P, _D, _I, _P, _P, _I, _P]),

@@ -1,10 +1,13 @@
 """Per-degree tile autotuner for the stage kernels.
 
 For a solver it times every compiled tile variant (elements per block x threads per
-block; degree-specialised FP32 variants and the generic kernel) over a few LSRK steps on the
-solver's own mesh with CUDA events, keeps the fastest, and caches the choice per
-(physics, N, dtype, element count, device name) in a JSON file next to the built library
-(the element count decides which tiles divide the mesh).
+block; every degree-specialised FP32 variant of its physics and degree in the library's
+registry, and the generic kernel's tiles) over a few LSRK steps on the solver's own mesh with
+CUDA events, keeps the fastest, and caches the choice per (physics, N, dtype, element count,
+device name, library content hash) in a JSON file next to the built library (the element
+count decides which tiles divide the mesh; a rebuilt library invalidates the entries). The
+field vector width is not a tuning dimension: it is fixed by the physics in the specialised
+kernels (wave: one 16-byte w entry per point; Maxwell: three 8-byte pieces).
 """
 from __future__ import annotations
 
@@ -17,33 +20,25 @@ from . import _build
 
 CACHE = os.path.join(_build.BUILD, "autotune.json")
 
-# Candidates (kernel, elements per block, threads per block).
-CANDIDATES = {
-    ("wave", 9, torch.float32): [("specialised", 4, 288), ("specialised", 4, 160),
-                                 ("specialised", 2, 160), ("generic", 4, 256)],
-    ("maxwell", 9, torch.float32): [("specialised", 2, 192), ("specialised", 2, 256),
-                                    ("generic", 2, 256)],
-    ("wave", 5, torch.float32): [("specialised", 4, 160), ("specialised", 8, 320),
-                                 ("specialised", 2, 96), ("generic", 8, 256)],
-    ("maxwell", 5, torch.float32): [("specialised", 4, 224), ("specialised", 8, 448),
-                                    ("specialised", 2, 128), ("generic", 8, 256)],
-    ("wave", 10, torch.float32): [("specialised", 2, 160), ("generic", 4, 256)],
-    ("maxwell", 10, torch.float32): [("specialised", 2, 192), ("specialised", 2, 256),
-                                     ("generic", 2, 256)],
-    ("wave", 4, torch.float32): [("specialised", 8, 320), ("generic", 8, 256)],
-    ("maxwell", 4, torch.float32): [("specialised", 4, 224), ("generic", 8, 256)],
-    ("wave", 6, torch.float32): [("specialised", 4, 160), ("specialised", 8, 320),
-                                 ("specialised", 2, 160), ("generic", 6, 256)],
-    ("maxwell", 6, torch.float32): [("specialised", 2, 192), ("generic", 6, 256)],
-    ("wave", 7, torch.float32): [("specialised", 4, 288), ("specialised", 2, 160),
-                                 ("generic", 6, 256)],
-    ("maxwell", 7, torch.float32): [("specialised", 2, 192), ("generic", 6, 256)],
-    ("wave", 8, torch.float32): [("specialised", 4, 288), ("generic", 4, 256)],
-    ("maxwell", 8, torch.float32): [("specialised", 4, 224), ("generic", 4, 256)],
-    ("wave", 11, torch.float32): [("specialised", 2, 224), ("generic", 2, 256)],
-    ("maxwell", 11, torch.float32): [("specialised", 2, 256), ("generic", 2, 256)],
-}
-GENERIC = [("generic", e, 256) for e in (1, 2, 4, 6, 12)]
+# Generic-kernel candidates (kernel, elements per block, threads per block); the
+# degree-specialised ones come from the library's registry of compiled variants.
+GENERIC = [("generic", e, 256) for e in (1, 2, 4, 6, 8, 12)]
+
+
+def compiled_variants():
+    """Every compiled degree-specialised variant: [(N, physics, elems_per_block, threads)]."""
+    import ctypes
+    from . import _lib
+    from .solver import PHYSICS
+    names = {code: name for name, (code, _) in PHYSICS.items()}
+    L = _lib.load()
+    out, idx = [], 0
+    vals = [ctypes.c_int() for _ in range(4)]
+    while L.bb_fast_variant(idx, *(ctypes.byref(v) for v in vals)) == 0:
+        N, phys, epb, nt = (v.value for v in vals)
+        out.append((N, names.get(phys, str(phys)), epb, nt))
+        idx += 1
+    return out
 
 
 _LIB_HASH = None
@@ -76,7 +71,13 @@ def _load():
 
 
 def candidates(solver):
-    return CANDIDATES.get((solver.physics, solver.N, solver.dtype), GENERIC)
+    """Every compiled specialised variant for the solver's (physics, N) whose tile divides
+    its element count (FP32 only), then the generic tiles; each is timed, the fastest kept."""
+    spec = []
+    if solver.dtype == torch.float32:
+        spec = [("specialised", epb, nt) for (N, phys, epb, nt) in compiled_variants()
+                if N == solver.N and phys == solver.physics and solver.K % epb == 0]
+    return spec + GENERIC
 
 
 def tune(solver, steps: int = 3, use_cache: bool = True, verbose: bool = False):

@@ -38,6 +38,24 @@ int bb_fast_variant_info(int idx, int* epb, int* threads, size_t* smem) {
   return BB_ERR_ARG;
 }
 
+// C ABI: the compiled variants, for tile choosers (the autotuner times every one that fits).
+extern "C" int bb_fast_variant(int idx, int* N, int* physics, int* epb, int* threads) {
+  if (!N || !physics || !epb || !threads) return BB_ERR_ARG;
+  int i = 0;
+#define BB_VAR(n_, p_, e_, t_)                        \
+  if (idx == i) {                                     \
+    *N = n_;                                          \
+    *physics = p_;                                    \
+    *epb = e_;                                        \
+    *threads = FastLayout<n_, p_, e_, t_>::NT;        \
+    return BB_OK;                                     \
+  }                                                   \
+  ++i;
+  BB_FAST_VARIANTS(BB_VAR)
+#undef BB_VAR
+  return BB_ERR_ARG;
+}
+
 int bb_fast_launch(int idx, const FastLaunch& fl, const FastStageParams& P, cudaStream_t st) {
   int i = 0;
 #define BB_LAUNCH(n_, p_, e_, t_)                                 \

@@ -122,6 +122,10 @@ int bb_solver_get_tile(const bb_solver* s, int* elems_per_block, int* threads);
 /* Shared memory of one generic-kernel tile of epb elements (and whether it runs the
  * chain-per-thread lift), for tile choosers. */
 int bb_stage_tile_bytes(int physics, int N, int dtype, int epb, int64_t* bytes, int* chain);
+/* The idx-th compiled degree-specialised FP32 stage-kernel variant (idx = 0, 1, ...): its
+ * degree, physics, elements per block and threads per block, for tile choosers; BB_ERR_ARG
+ * past the last one. No counterpart in the reference (a tuning aid). */
+int bb_fast_variant(int idx, int* N, int* physics, int* elems_per_block, int* threads);
 /* kind 0: use a degree-specialised kernel when one exists (default); 1: generic kernel. */
 int bb_solver_set_kernel(bb_solver* s, int kind);
 /* 0 if a degree-specialised kernel is in use, 1 for the generic kernel. */

@@ -410,3 +410,18 @@ def test_checkpoint_resume_is_bitwise_and_fp64_dump_seeds_fp32(cuda, bb, tmp_pat
     other = bb.DGSolver(m, 5, "maxwell", dtype=torch.float32, tau=1.0)
     with pytest.raises(ValueError):
         other.load_state(str(tmp_path / "ck.npz"))
+
+
+def test_autotuner_keeps_the_fastest_candidate_it_timed(cuda, bb):
+    """tune() times every candidate that runs (every compiled specialised variant of the
+    physics and degree that divides K, and the generic tiles) and keeps the fastest."""
+    import torch
+    from bbdg import autotune
+    m = bb.uniform_tet_mesh(8)
+    s = bb.DGSolver(m, 9, "wave", dtype=torch.float32, tau=1.0)
+    (kind, epb, nt), table = autotune.tune(s, steps=2, use_cache=False)
+    names = {f"{k}:{e}x{t}" for k, e, t in autotune.candidates(s)}
+    assert {n for n in names if n.startswith("specialised")} <= set(table)
+    best = min(table, key=table.get)
+    assert best == f"{kind}:{epb}x{nt}"
+    assert s.kernel == kind and s.tile == (epb, nt)

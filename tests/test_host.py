@@ -204,3 +204,30 @@ def test_stack_slot_header_is_generated_and_injective():
         assert max(slots) + 1 == span
         nps = (max(NP, span) + 14) // 16 * 16 + 1
         assert span <= nps and nps % 16 == 1
+
+
+def test_autotuner_candidates_come_from_the_compiled_registry(monkeypatch):
+    """The autotuner's specialised candidates are the library's compiled variants (read
+    through bb_fast_variant, no GPU needed), and its cache key changes with the library's
+    content hash, so a rebuilt library is tuned again."""
+    torch = pytest.importorskip("torch")
+    from bbdg import autotune
+    variants = autotune.compiled_variants()
+    assert len(variants) >= 20 and len(set(variants)) == len(variants)
+    header = open(os.path.join(os.path.dirname(__file__), "..", "bernsteinbasis.jl_gb300",
+                               "csrc", "bbdg_stage_fast_variants.h")).read()
+    listed = re.findall(r"X\((\d+), BB_(WAVE|MAXWELL), (\d+), (\d+)\)", header)
+    assert [(int(n), p.lower(), int(e)) for n, p, e, _ in listed] == \
+        [(n, p, e) for n, p, e, _ in variants]
+
+    class FakeSolver:
+        physics, N, dtype, K, device = "wave", 9, torch.float32, 3072, None
+    monkeypatch.setattr(torch.cuda, "get_device_name", lambda d=None: "GPU")
+    monkeypatch.setattr(autotune, "_LIB_HASH", "aaaa")
+    k1 = autotune._key(FakeSolver)
+    monkeypatch.setattr(autotune, "_LIB_HASH", "bbbb")
+    assert autotune._key(FakeSolver) != k1
+    cands = autotune.candidates(FakeSolver)
+    spec = [c for c in cands if c[0] == "specialised"]
+    assert spec == [("specialised", e, t) for n, p, e, t in variants
+                    if n == 9 and p == "wave" and 3072 % e == 0]
