@@ -346,7 +346,9 @@ def main():
                        "parallelism": f"replicas x{world}",
                        "tile": {"kernel": kind, "elems_per_block": epb, "threads": nt},
                        "autotune_ms_per_step": tune_table,
-                       "l2": "inputs larger than L2 (q 0.69 GB + res 0.69 GB + traces per GPU, L2 129 MB)"},
+                       "l2": f"inputs larger than L2 (q {state_bytes / 1e9:.2f} GB + res "
+                             f"{state_bytes / 1e9:.2f} GB + traces per GPU, L2 129 MB)"
+                             if 2 * state_bytes > 129e6 else "inputs fit in L2 (profiling case)"},
             "e2e": {"value": e2e_value, "unit": "DOF-steps/s",
                     "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes},
             "gpu_launches": int(launches),
