@@ -12,7 +12,9 @@
 // its four stack entries in the reference's face order (t=-1 face first, then faces 1, 2, 3 through
 // the permutations of src/BernsteinLift.jl:207-218) and stores it coalesced. No atomics, so the
 // result does not depend on scheduling. The next tile's inputs arrive while this tile is worked on:
-// in registers (degrees up to 9) or by a bulk copy into their own buffer (degrees 10 to 12).
+// in registers (degrees up to 9), by a bulk copy into their own buffer (degrees 10 and 11), or
+// from 12 on pulled into L2 a tile ahead and read with coalesced loads into the stack area at the
+// start of the tile (no input buffer, so more elements per warp fit: 4 up to N = 13).
 //
 // Single-face lift (face_lift_multiply!): the t = -1 face's stack is already in volume order, so
 // the chain writes the output tile directly.
@@ -88,22 +90,28 @@ struct Lift4 {
   static constexpr int NPS = NP | 1;    // stack stride: odd, conflict-free stack stores
   static constexpr int NFPP = NFP | 1;  // input row stride when staged from registers
   // elements per warp: 8 (32 chains) while the stacks leave room for several warps per SM;
-  // 4 (16 chains, half the lanes idle in the chain phase) from N = 11 on and 2 from N = 13
+  // 4 (16 chains, half the lanes idle in the chain phase) from N = 11 on and 2 from N = 14
   // on, which keeps several warps per SM for the loads and the gather (measured at N = 11
-  // and 12: +16 %, +17 %; at N = 10 -15 %)
-  static constexpr int EPW = N >= 13 ? 2 : N >= 11 ? 4 : 8;
+  // and 12: +16 %, +17 %; at N = 10 -15 %; at N = 13 with the staged inputs 4 beats 2 by 14 %,
+  // at N = 14 and 15 2 beats 4 and 8)
+  static constexpr int EPW = N >= 14 ? 2 : N >= 11 ? 4 : 8;
+  // from N = 12: the next tile's inputs go to L2 (bulk prefetch), this tile's are read with
+  // coalesced 16-byte loads and staged through the stack area (N = 12: 0.29 -> 0.31 of the
+  // HBM copy rate, N = 13: 0.20 -> 0.235; slower at N = 10, 11 than the bulk-copy buffer)
+  static constexpr bool STAGED = N >= 12;
   static constexpr int INW = EPW * 4 * NFP;  // input floats per tile
   // next tile in registers when they fit beside the chain, else a bulk copy
   static constexpr bool REG_PREFETCH = N <= 9;
   static constexpr int NV4 = (INW / 4 + 31) / 32;  // float4 inputs per lane
   // shared memory, bytes: [bulk input buffer][stacks (also the register-staged input)][perm]
-  static constexpr int IN_B = REG_PREFETCH ? 0 : INW * 4;
+  static constexpr int IN_B = (REG_PREFETCH || STAGED) ? 0 : INW * 4;
   static constexpr int G_B = IN_B;
   static constexpr int P_B = G_B + (EPW * 4 * NPS * 4 + 15) / 16 * 16;
   static constexpr int BAR_B = P_B + (NP * 4 + 15) / 16 * 16;
   static constexpr int SMEM = BAR_B + 16;
   static_assert(NFPP <= NPS, "staged inputs fit in the stack area");
   static_assert(REG_PREFETCH ? EPW == 8 : true, "the register path stages 32 chains");
+  static_assert(EPW * 4 <= 32, "one chain per lane");
   static_assert(NP < 1024, "stack positions are packed in 10 bits");
   static_assert(INW % 4 == 0 && (INW * 4) % 16 == 0, "tiles are whole 16-byte chunks");
 };
@@ -170,7 +178,7 @@ __global__ void __launch_bounds__(32) lift4_kernel(int64_t K, const float* __res
   };
   if constexpr (L::REG_PREFETCH) {
     if (blockIdx.x < ntile) fetch(blockIdx.x);
-  } else {
+  } else if constexpr (!L::STAGED) {
     if (t == 0) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(lf_saddr(bar)) : "memory");
       asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -204,6 +212,44 @@ __global__ void __launch_bounds__(32) lift4_kernel(int64_t K, const float* __res
       for (int m = 0; m < NFP; ++m) X[m] = sG[t * NFPP + m];
       __syncwarp();  // every staged input is in registers before the stacks overwrite them
       if (next < ntile) fetch(next);
+    } else if constexpr (L::STAGED) {
+      // the tile's inputs, pulled into L2 a tile ago: coalesced 16-byte loads, staged in the
+      // stack area (free until the chains write it) in rows of NFPP, then one row per lane
+      const float4* xs = reinterpret_cast<const float4*>(x + tile * EPW * 4 * NFP);
+      const int nv = ne * NFP;  // float4s of the tile (4 NFP floats per element)
+      constexpr int UNR = 8;
+      for (int v0 = 0; v0 < nv; v0 += 32 * UNR) {
+        float4 buf[UNR];
+#pragma unroll
+        for (int r = 0; r < UNR; ++r) {
+          const int v = v0 + t + 32 * r;
+          if (v < nv) buf[r] = __ldg(xs + v);
+        }
+#pragma unroll
+        for (int r = 0; r < UNR; ++r) {
+          const int v = v0 + t + 32 * r;
+          if (v < nv) {
+            const float qq[4] = {buf[r].x, buf[r].y, buf[r].z, buf[r].w};
+#pragma unroll
+            for (int w = 0; w < 4; ++w) {
+              const int g = 4 * v + w, ch = g / NFP, m = g - ch * NFP;
+              sG[ch * NFPP + m] = qq[w];
+            }
+          }
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int m = 0; m < NFP; ++m) X[m] = sG[(t < ne * 4 ? t : 0) * NFPP + m];
+      __syncwarp();  // every staged input is in registers before the stacks overwrite them
+      if (t == 0 && next < ntile) {
+        // 16-byte aligned start and size: x is (checked by the caller) and a tile is
+        // EPW * 4 * NFP floats, a multiple of 4
+        const uint32_t bytes = (uint32_t)(tile_ne(next) * 4 * NFP * 4);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(x + next * EPW * 4 * NFP),
+                     "r"(bytes)
+                     : "memory");
+      }
     } else {
       if (!wait_in(ph)) {
         if (t == 0) {
