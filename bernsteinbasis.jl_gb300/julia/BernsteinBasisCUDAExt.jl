@@ -26,6 +26,7 @@ const BB_F64 = Cint(1)
 const BB_WAVE = Cint(0)
 const BB_MAXWELL = Cint(1)
 const BB_ADVECTION = Cint(2)   # examples/3d_advec_scalar.jl
+const BB_ADVECTION3 = Cint(3)  # examples/3d_advec.jl (u, v, w)
 
 dtype_code(::Type{Float32}) = BB_F32
 dtype_code(::Type{Float64}) = BB_F64
@@ -96,8 +97,8 @@ end
 function BBSolver(physics::Symbol, N::Integer, conn::CuVector{Int32}, geo::CuVector{T};
                   tau::Real = 1.0) where {T<:Union{Float32,Float64}}
     code = physics === :wave ? BB_WAVE : physics === :maxwell ? BB_MAXWELL :
-           physics === :advection ? BB_ADVECTION :
-           throw(ArgumentError("physics must be :wave, :maxwell or :advection"))
+           physics === :advection ? BB_ADVECTION : physics === :advection3 ? BB_ADVECTION3 :
+           throw(ArgumentError("physics must be :wave, :maxwell, :advection or :advection3"))
     r = Ref{Ptr{Cvoid}}(C_NULL)
     K = length(conn) ÷ 4
     check(ccall((:bb_solver_create, libbbdg), Cint,
