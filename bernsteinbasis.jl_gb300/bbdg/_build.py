@@ -3,6 +3,11 @@
 Each translation unit under ``csrc/`` is compiled in parallel with
 ``nvcc -gencode arch=compute_103a,code=sm_103a -O3 -lineinfo`` and linked into
 ``_build/libbbdg.so`` next to this package (static CUDA runtime, no torch dependency).
+
+With ``BBDG_DEBUG=1`` in the environment the debug build is made and loaded instead:
+``-DBB_DEBUG_CHECKS`` into ``_build_debug/libbbdg.so``. Its kernels check their
+table-derived and neighbour indices, set a status bit on a violation and skip the access
+(reported as BB_ERR_DEVICE, "debug index check failed"); nothing traps.
 """
 from __future__ import annotations
 
@@ -16,7 +21,8 @@ import sys
 PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(PKG_ROOT, "csrc")
 INCLUDE = os.path.join(os.path.dirname(PKG_ROOT), "include")
-BUILD = os.path.join(PKG_ROOT, "_build")
+DEBUG = os.environ.get("BBDG_DEBUG", "") == "1"
+BUILD = os.path.join(PKG_ROOT, "_build_debug" if DEBUG else "_build")
 LIB = os.path.join(BUILD, "libbbdg.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -51,6 +57,8 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     cc = nvcc()
     flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
                     "-I", INCLUDE, "--expt-relaxed-constexpr"] + list(extra_flags)
+    if DEBUG:
+        flags.append("-DBB_DEBUG_CHECKS")
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")

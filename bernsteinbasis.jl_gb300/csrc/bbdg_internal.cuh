@@ -137,8 +137,18 @@ int bb_set_device(bb_ctx* ctx);
 int bb_check_launch(bb_ctx* ctx, const char* what);
 // Error for a nonzero device status word. Bit 0: a kernel found corrupt connectivity (a
 // neighbour index or orientation out of range) and skipped the access; bit 1: a bounded
-// device-side wait ran out and the kernel returned early. A time-out takes precedence.
+// device-side wait ran out and the kernel returned early; bit 2: a debug index check failed
+// (debug builds only). A time-out takes precedence.
 int bb_device_status_error(bb_ctx* ctx, int word);
+
+// Debug index checks, compiled in with -DBB_DEBUG_CHECKS (the BBDG_DEBUG=1 build): a
+// table-derived or neighbour index outside its range sets bit 2 of the status word and the
+// access is skipped; nothing traps. Off in the normal build, where the tables are trusted.
+#ifdef BB_DEBUG_CHECKS
+#define BB_DCHECK(cond, status) ((cond) ? true : (atomicOr((status), 4), false))
+#else
+#define BB_DCHECK(cond, status) true
+#endif
 
 inline size_t dtype_size(int dtype) { return dtype == BB_F64 ? 8 : 4; }
 // Fields of a physics code, 0 if unknown.

@@ -40,6 +40,8 @@ int bb_check_launch(bb_ctx* ctx, const char* what) {
 int bb_device_status_error(bb_ctx* ctx, int word) {
   if (word & 2)
     return bb_fail(ctx, BB_ERR_TIMEOUT, "a device-side bounded wait ran out (status 0x%x)", word);
+  if (word & 4)
+    return bb_fail(ctx, BB_ERR_DEVICE, "debug index check failed (status 0x%x)", word);
   return bb_fail(ctx, BB_ERR_DEVICE, "device check failed: corrupt connectivity (status 0x%x)",
                  word);
 }

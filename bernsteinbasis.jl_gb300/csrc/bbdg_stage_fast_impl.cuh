@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
 #pragma unroll
     for (int r = 0; r < FR; ++r) {
       const int a = fa0 + r * FT;
-      if (a < NFP && !inside && !bad) {
+      if (a < NFP && !inside && !bad && BB_DCHECK(sFperm[o * NFP + a] < NFP, P.status)) {
         const float* tp = tbase + sFperm[o * NFP + a];
 #pragma unroll
         for (int m = 0; m < NF; ++m) tr[r][m] = __ldg(tp + m * NFP);
@@ -436,7 +436,13 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
       if (a >= NFP) continue;
       float d[NF];
       const float* qM = sQ + le * NP + sFvol[ff * NFP + a];
-      if (bad) {
+      // debug builds: every table-derived node index in range (else the node's jump is 0)
+      const bool dbad =
+          !BB_DCHECK(sFvol[ff * NFP + a] < NP &&
+                         (inside ? sFnb[(nface * 6 + o) * NFP + a] < NP
+                                 : sFperm[o * NFP + a] < NFP),
+                     P.status);
+      if (bad || dbad) {
 #pragma unroll
         for (int m = 0; m < NF; ++m) d[m] = 0.f;
       } else if (inside) {

@@ -237,10 +237,13 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
       if (nbr >= K || o > 5) {
         atomicOr(P.status, 1);
         for (int fld = 0; fld < NF; ++fld) d[fld] = T(0);
+      } else if (!BB_DCHECK(vM < Np && st.fperm[o * Nfp + a] < Nfp, P.status)) {
+        for (int fld = 0; fld < NF; ++fld) d[fld] = T(0);
       } else {
         const int ap = st.fperm[o * Nfp + a];
         if (nbr >= e0 && nbr < e0 + ne) {
-          const int vP = st.fvol[nface * Nfp + ap];
+          const int vP = BB_DCHECK(st.fvol[nface * Nfp + ap] < Np, P.status)
+                             ? st.fvol[nface * Nfp + ap] : vM;
           const T* qP = sQ + (size_t)(nbr - e0) * Np + vP;
           const T* qM = sQ + (size_t)le * Np + vM;
 #pragma unroll
@@ -251,7 +254,8 @@ __device__ void generic_stage_tile(const StageParams<T>& P, const TileLayout& L,
 #pragma unroll
           for (int fld = 0; fld < NF; ++fld) d[fld] = __ldg(tp + (size_t)fld * Nfp) - qM[(size_t)fld * epb * Np];
         } else {
-          const int vP = st.fvol[nface * Nfp + ap];
+          const int vP = BB_DCHECK(st.fvol[nface * Nfp + ap] < Np, P.status)
+                             ? st.fvol[nface * Nfp + ap] : vM;
           const T* qP = P.q + (size_t)nbr * Np + vP;
           const T* qM = sQ + (size_t)le * Np + vM;
 #pragma unroll

@@ -231,3 +231,23 @@ def test_autotuner_candidates_come_from_the_compiled_registry(monkeypatch):
     spec = [c for c in cands if c[0] == "specialised"]
     assert spec == [("specialised", e, t) for n, p, e, t in variants
                     if n == 9 and p == "wave" and 3072 % e == 0]
+
+
+def test_debug_index_checks_compile():
+    """The debug build's index checks (-DBB_DEBUG_CHECKS) compile in the stage kernels: the
+    generic tile (bbdg_solver.cu) and the degree-specialised N = 9 variants."""
+    import shutil
+    import subprocess
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not found")
+    csrc = os.path.join(os.path.dirname(__file__), "..", "bernsteinbasis.jl_gb300", "csrc")
+    inc = os.path.join(os.path.dirname(__file__), "..", "include")
+    import tempfile
+    with tempfile.TemporaryDirectory() as tmp:
+        for src in ("bbdg_solver.cu", "bbdg_stage_fast_v9.cu"):
+            r = subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O1",
+                                "-std=c++17", "-I", inc, "--expt-relaxed-constexpr",
+                                "-DBB_DEBUG_CHECKS", "-c", os.path.join(csrc, src), "-o",
+                                os.path.join(tmp, src + ".o")], capture_output=True, text=True)
+            assert r.returncode == 0, r.stderr[-2000:]
