@@ -2,6 +2,7 @@
 // examples. The generic (runtime-degree) stage tile is in bbdg_stage_generic.cuh, the
 // degree-specialised FP32 kernels in bbdg_stage_fast.cu; this file owns trace buffers,
 // kernel selection, LSRK stepping and CUDA graphs.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -18,20 +19,23 @@ __global__ void __launch_bounds__(kThreads) stage_kernel(StageParams<T> P, TileL
   extern __shared__ __align__(16) unsigned char smem[];
   const SmemTables st =
       load_tables(P.tab, P.gtab, reinterpret_cast<uint32_t*>(smem + L.tab_bytes));
-  const int64_t ntiles = (P.K + P.epb - 1) / P.epb;
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+  const int64_t ntiles = P.tile_end > 0 ? P.tile_end : (P.K + P.epb - 1) / P.epb;
+  for (int64_t tile = P.tile_begin + blockIdx.x; tile < ntiles; tile += gridDim.x)
     generic_stage_tile<T, PHYS>(P, L, st, tile);
 }
 
-// Writes every face trace of q (all faces) into the trace buffer.
+// Writes every face trace (all faces) of elements [e_begin, e_end) of q into the trace buffer.
 template <class T, int NF>
 __global__ void extract_traces_kernel(DegTables tab, const uint32_t* __restrict__ gtab,
-                                      int64_t K, const T* __restrict__ q, T* __restrict__ tr) {
+                                      int64_t K, const T* __restrict__ q, T* __restrict__ tr,
+                                      int64_t e_begin, int64_t e_end) {
   const int Np = tab.Np, Nfp = tab.Nfp;
   const uint16_t* fvol = reinterpret_cast<const uint16_t*>(gtab + tab.o_fvol);
-  const int64_t total = K * 4 * NF * Nfp;
-  for (int64_t it = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; it < total;
-       it += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t first = e_begin * 4 * NF * Nfp;
+  const int64_t total = (e_end - e_begin) * 4 * NF * Nfp;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t it = first + i;
     const int64_t e = it / (4 * NF * Nfp);
     int rem = (int)(it - e * 4 * NF * Nfp);
     const int f = rem / (NF * Nfp);
@@ -72,6 +76,8 @@ struct bb_solver {
   size_t trace_bytes = 0;
   int* d_status = nullptr;
   cudaStream_t cap_stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // bb_lsrk_run_host's upload/download stream
+  cudaEvent_t copy_ev[2 * 4 + 2] = {};  // its events (4 = kHostChunks)
   // graph cache: one graph per starting trace buffer parity
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   void* g_q = nullptr;
@@ -102,14 +108,18 @@ int solver_layout(bb_solver* s, int epb, size_t* smem_out, int* chain_out = null
   return L.total <= s->ctx->smem_optin ? BB_OK : BB_ERR_ARG;
 }
 
+// tb, te: the launch covers tiles [tb, te) of the solver's tile size (te = 0: all tiles).
 template <class T, int PHYS>
 int launch_stage_t(bb_solver* s, int mode, int stage, double dt, void* q, void* res, void* rhs,
-                   const void* tin, void* tout, cudaStream_t st) {
+                   const void* tin, void* tout, cudaStream_t st, int64_t tb = 0,
+                   int64_t te = 0) {
   bb_ctx* ctx = s->ctx;
   StageParams<T> P;
   P.tab = *s->tab;
   P.gtab = s->tab->d_words;
   P.K = s->K;
+  P.tile_begin = tb;
+  P.tile_end = te;
   P.epb = s->epb;
   P.mode = mode;
   P.rkA = T(mode ? kRK4A[stage] : 0.0);
@@ -132,7 +142,8 @@ int launch_stage_t(bb_solver* s, int mode, int stage, double dt, void* q, void* 
   BB_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stage_kernel<T, PHYS>,
                                                              kThreads, L.total));
   if (per_sm < 1) return bb_fail(ctx, BB_ERR_ARG, "tile does not fit on an SM");
-  const int64_t ntiles = (s->K + s->epb - 1) / s->epb;
+  const int64_t ntiles = (te > 0 ? te : (s->K + s->epb - 1) / s->epb) - tb;
+  if (ntiles < 1) return bb_fail(ctx, BB_ERR_ARG, "empty tile range");
   int64_t grid = (int64_t)per_sm * ctx->num_sms;
   if (grid > ntiles) grid = ntiles;
   stage_kernel<T, PHYS><<<(int)grid, kThreads, L.total, st>>>(P, L);
@@ -140,7 +151,7 @@ int launch_stage_t(bb_solver* s, int mode, int stage, double dt, void* q, void* 
 }
 
 int launch_fast(bb_solver* s, int mode, int stage, double dt, void* q, void* res, void* rhs,
-                const void* tin, void* tout, cudaStream_t st) {
+                const void* tin, void* tout, cudaStream_t st, int64_t tb = 0, int64_t te = 0) {
   FastStageParams P;
   const DegTables& t = *s->tab;
   P.gtab = t.d_words;
@@ -150,6 +161,8 @@ int launch_fast(bb_solver* s, int mode, int stage, double dt, void* q, void* res
   P.o_fperm = t.o_fperm;
   P.o_sslot = t.o_sslot;
   P.K = s->K;
+  P.tile_begin = tb;
+  P.tile_end = te;
   P.mode = mode;
   P.rkA = float(mode ? kRK4A[stage] : 0.0);
   P.rkB = float(mode ? kRK4B[stage] : 0.0);
@@ -176,53 +189,56 @@ int launch_fast(bb_solver* s, int mode, int stage, double dt, void* q, void* res
 bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
 
 int launch_stage(bb_solver* s, int mode, int stage, double dt, void* q, void* res, void* rhs,
-                 const void* tin, void* tout, cudaStream_t st) {
+                 const void* tin, void* tout, cudaStream_t st, int64_t tb = 0, int64_t te = 0) {
   // the specialised kernels move tiles with 16-byte-aligned bulk copies and store q, res
   // and rhs with 16-byte vector stores
   if (s->fast >= 0 && aligned16(q) && (!res || aligned16(res)) && (!rhs || aligned16(rhs)) &&
       aligned16(s->geo) && aligned16(s->conn))
-    return launch_fast(s, mode, stage, dt, q, res, rhs, tin, tout, st);
+    return launch_fast(s, mode, stage, dt, q, res, rhs, tin, tout, st, tb, te);
   if (s->physics == BB_WAVE)
     return s->dtype == BB_F64
-               ? launch_stage_t<double, BB_WAVE>(s, mode, stage, dt, q, res, rhs, tin, tout, st)
-               : launch_stage_t<float, BB_WAVE>(s, mode, stage, dt, q, res, rhs, tin, tout, st);
+               ? launch_stage_t<double, BB_WAVE>(s, mode, stage, dt, q, res, rhs, tin, tout, st, tb, te)
+               : launch_stage_t<float, BB_WAVE>(s, mode, stage, dt, q, res, rhs, tin, tout, st, tb, te);
   if (s->physics == BB_ADVECTION)
     return s->dtype == BB_F64
-               ? launch_stage_t<double, BB_ADVECTION>(s, mode, stage, dt, q, res, rhs, tin, tout, st)
-               : launch_stage_t<float, BB_ADVECTION>(s, mode, stage, dt, q, res, rhs, tin, tout, st);
+               ? launch_stage_t<double, BB_ADVECTION>(s, mode, stage, dt, q, res, rhs, tin, tout, st, tb, te)
+               : launch_stage_t<float, BB_ADVECTION>(s, mode, stage, dt, q, res, rhs, tin, tout, st, tb, te);
   if (s->physics == BB_ADVECTION3)
     return s->dtype == BB_F64
-               ? launch_stage_t<double, BB_ADVECTION3>(s, mode, stage, dt, q, res, rhs, tin, tout, st)
-               : launch_stage_t<float, BB_ADVECTION3>(s, mode, stage, dt, q, res, rhs, tin, tout, st);
+               ? launch_stage_t<double, BB_ADVECTION3>(s, mode, stage, dt, q, res, rhs, tin, tout, st, tb, te)
+               : launch_stage_t<float, BB_ADVECTION3>(s, mode, stage, dt, q, res, rhs, tin, tout, st, tb, te);
   return s->dtype == BB_F64
-             ? launch_stage_t<double, BB_MAXWELL>(s, mode, stage, dt, q, res, rhs, tin, tout, st)
-             : launch_stage_t<float, BB_MAXWELL>(s, mode, stage, dt, q, res, rhs, tin, tout, st);
+             ? launch_stage_t<double, BB_MAXWELL>(s, mode, stage, dt, q, res, rhs, tin, tout, st, tb, te)
+             : launch_stage_t<float, BB_MAXWELL>(s, mode, stage, dt, q, res, rhs, tin, tout, st, tb, te);
 }
 
-int launch_extract(bb_solver* s, const void* q, void* tr, cudaStream_t st) {
-  const int64_t total = s->K * 4 * s->nf * s->tab->Nfp;
+// Traces of elements [e0, e1) (e1 = -1: to the end).
+int launch_extract(bb_solver* s, const void* q, void* tr, cudaStream_t st, int64_t e0 = 0,
+                   int64_t e1 = -1) {
+  if (e1 < 0) e1 = s->K;
+  const int64_t total = (e1 - e0) * 4 * s->nf * s->tab->Nfp;
   int64_t grid = (total + 255) / 256;
   if (grid > (int64_t)s->ctx->num_sms * 16) grid = (int64_t)s->ctx->num_sms * 16;
   if (grid < 1) grid = 1;
   const DegTables& t = *s->tab;
   if (s->dtype == BB_F64) {
     if (s->nf == 4)
-      extract_traces_kernel<double, 4><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr);
+      extract_traces_kernel<double, 4><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr, e0, e1);
     else if (s->nf == 1)
-      extract_traces_kernel<double, 1><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr);
+      extract_traces_kernel<double, 1><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr, e0, e1);
     else if (s->nf == 3)
-      extract_traces_kernel<double, 3><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr);
+      extract_traces_kernel<double, 3><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr, e0, e1);
     else
-      extract_traces_kernel<double, 6><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr);
+      extract_traces_kernel<double, 6><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr, e0, e1);
   } else {
     if (s->nf == 4)
-      extract_traces_kernel<float, 4><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr);
+      extract_traces_kernel<float, 4><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr, e0, e1);
     else if (s->nf == 1)
-      extract_traces_kernel<float, 1><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr);
+      extract_traces_kernel<float, 1><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr, e0, e1);
     else if (s->nf == 3)
-      extract_traces_kernel<float, 3><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr);
+      extract_traces_kernel<float, 3><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr, e0, e1);
     else
-      extract_traces_kernel<float, 6><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr);
+      extract_traces_kernel<float, 6><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr, e0, e1);
   }
   return bb_check_launch(s->ctx, "extract_traces_kernel");
 }
@@ -363,6 +379,9 @@ extern "C" int bb_solver_destroy(bb_solver* s) {
   cudaFree(s->trace[1]);
   cudaFree(s->d_status);
   if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
+  if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
+  for (auto& e : s->copy_ev)
+    if (e) cudaEventDestroy(e);
   delete s;
   return BB_OK;
 }
@@ -456,18 +475,12 @@ extern "C" int bb_solver_check(bb_solver* s, void* stream) {
   return check_status(s, (cudaStream_t)stream);
 }
 
-extern "C" int bb_lsrk_run(bb_solver* s, double dt, int nsteps, void* q, void* res, int use_graph,
-                           void* stream) {
-  if (!s || !q || !res) return s ? bb_fail(s->ctx, BB_ERR_ARG, "null pointer") : BB_ERR_ARG;
-  if (nsteps < 0 || !std::isfinite(dt)) return bb_fail(s->ctx, BB_ERR_ARG, "bad dt or nsteps");
-  if (q == res) return bb_fail(s->ctx, BB_ERR_ARG, "res must not alias q");
-  int rc = bb_set_device(s->ctx);
-  if (rc) return rc;
-  if (nsteps == 0) return BB_OK;
-  cudaStream_t st = (cudaStream_t)stream;
-  // traces of the incoming state; stage kernels then keep them current
-  rc = launch_extract(s, q, s->trace[0], st);
-  if (rc) return rc;
+namespace {
+
+// nsteps LSRK steps from traces of q already current in trace buffer 0.
+int run_steps(bb_solver* s, double dt, int nsteps, void* q, void* res, int use_graph,
+              cudaStream_t st) {
+  int rc = BB_OK;
   if (use_graph) {
     if (s->g_q != q || s->g_res != res || s->g_dt != dt || s->g_epb != s->epb ||
         s->g_epoch != s->ctx->config_epoch)
@@ -495,18 +508,115 @@ extern "C" int bb_lsrk_run(bb_solver* s, double dt, int nsteps, void* q, void* r
   return BB_OK;
 }
 
+// The host-buffer path's second stream and its events, made on first use.
+constexpr int kHostChunks = 4;
+static_assert(sizeof(bb_solver::copy_ev) / sizeof(cudaEvent_t) == 2 * kHostChunks + 2,
+              "one start, kHostChunks upload, kHostChunks compute and one done event");
+int ensure_copy_stream(bb_solver* s) {
+  if (s->copy_stream) return BB_OK;
+  for (auto& e : s->copy_ev)
+    if (!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+      return bb_fail(s->ctx, BB_ERR_CUDA, "copy event creation failed");
+  cudaStream_t cs = nullptr;
+  if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
+    return bb_fail(s->ctx, BB_ERR_CUDA, "copy stream creation failed");
+  s->copy_stream = cs;
+  return BB_OK;
+}
+
+}  // namespace
+
+extern "C" int bb_lsrk_run(bb_solver* s, double dt, int nsteps, void* q, void* res, int use_graph,
+                           void* stream) {
+  if (!s || !q || !res) return s ? bb_fail(s->ctx, BB_ERR_ARG, "null pointer") : BB_ERR_ARG;
+  if (nsteps < 0 || !std::isfinite(dt)) return bb_fail(s->ctx, BB_ERR_ARG, "bad dt or nsteps");
+  if (q == res) return bb_fail(s->ctx, BB_ERR_ARG, "res must not alias q");
+  int rc = bb_set_device(s->ctx);
+  if (rc) return rc;
+  if (nsteps == 0) return BB_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  // traces of the incoming state; stage kernels then keep them current
+  rc = launch_extract(s, q, s->trace[0], st);
+  if (rc) return rc;
+  return run_steps(s, dt, nsteps, q, res, use_graph, st);
+}
+
+// Host state in and out, pipelined: the state goes up in kHostChunks element ranges on a
+// second stream, and each range's traces are extracted as soon as it has landed; the steps
+// run as in bb_lsrk_run except the last stage of the last step, which runs range by range so
+// that each range's download starts while the later ranges are still being computed. The
+// caller's stream waits for the last download, so the call stays stream-ordered.
 extern "C" int bb_lsrk_run_host(bb_solver* s, double dt, int nsteps, const void* q_host_in,
                                 void* q_host_out, void* q_dev, void* res_dev, int use_graph,
                                 void* stream) {
   if (!s || !q_host_in || !q_host_out || !q_dev || !res_dev)
     return s ? bb_fail(s->ctx, BB_ERR_ARG, "null pointer") : BB_ERR_ARG;
+  if (nsteps < 0 || !std::isfinite(dt)) return bb_fail(s->ctx, BB_ERR_ARG, "bad dt or nsteps");
+  if (q_dev == res_dev) return bb_fail(s->ctx, BB_ERR_ARG, "res must not alias q");
   int rc = bb_set_device(s->ctx);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
-  const size_t bytes = (size_t)s->nf * s->K * s->tab->Np * dtype_size(s->dtype);
-  BB_CUDA(s->ctx, cudaMemcpyAsync(q_dev, q_host_in, bytes, cudaMemcpyHostToDevice, st));
-  rc = bb_lsrk_run(s, dt, nsteps, q_dev, res_dev, use_graph, st);
+  const size_t esz = dtype_size(s->dtype);
+  const size_t row = (size_t)s->tab->Np * esz;  // one element of one field
+  const size_t bytes = (size_t)s->nf * s->K * row;
+  if (nsteps == 0) {
+    BB_CUDA(s->ctx, cudaMemcpyAsync(q_dev, q_host_in, bytes, cudaMemcpyHostToDevice, st));
+    BB_CUDA(s->ctx, cudaMemcpyAsync(q_host_out, q_dev, bytes, cudaMemcpyDeviceToHost, st));
+    return BB_OK;
+  }
+  rc = ensure_copy_stream(s);
   if (rc) return rc;
-  BB_CUDA(s->ctx, cudaMemcpyAsync(q_host_out, q_dev, bytes, cudaMemcpyDeviceToHost, st));
+  cudaStream_t cs = s->copy_stream;
+  cudaEvent_t* ev = s->copy_ev;  // [0] start, [1..C] uploaded, [C+1..2C] computed, [2C+1] done
+  // ranges of whole tiles (the specialised kernels need them); empty ranges are skipped
+  const int64_t ntiles = (s->K + s->epb - 1) / s->epb;
+  int64_t tb[kHostChunks + 1], eb[kHostChunks + 1];
+  for (int c = 0; c <= kHostChunks; ++c) {
+    tb[c] = ntiles * c / kHostChunks;
+    eb[c] = std::min<int64_t>(s->K, tb[c] * s->epb);
+  }
+  char* qd = static_cast<char*>(q_dev);
+  const char* hin = static_cast<const char*>(q_host_in);
+  char* hout = static_cast<char*>(q_host_out);
+  BB_CUDA(s->ctx, cudaEventRecord(ev[0], st));
+  BB_CUDA(s->ctx, cudaStreamWaitEvent(cs, ev[0], 0));
+  for (int c = 0; c < kHostChunks; ++c) {
+    if (eb[c] == eb[c + 1]) continue;
+    for (int f = 0; f < s->nf; ++f) {
+      const size_t off = ((size_t)f * s->K + eb[c]) * row;
+      BB_CUDA(s->ctx, cudaMemcpyAsync(qd + off, hin + off, (eb[c + 1] - eb[c]) * row,
+                                      cudaMemcpyHostToDevice, cs));
+    }
+    BB_CUDA(s->ctx, cudaEventRecord(ev[1 + c], cs));
+    BB_CUDA(s->ctx, cudaStreamWaitEvent(st, ev[1 + c], 0));
+    rc = launch_extract(s, q_dev, s->trace[0], st, eb[c], eb[c + 1]);
+    if (rc) return rc;
+  }
+  if (nsteps > 1) {
+    rc = run_steps(s, dt, nsteps - 1, q_dev, res_dev, use_graph, st);
+    if (rc) return rc;
+  }
+  const int par = (nsteps - 1) & 1;
+  for (int stage = 0; stage < 4; ++stage) {
+    const int in = (par + stage) & 1;
+    rc = launch_stage(s, 1, stage, dt, q_dev, res_dev, nullptr, s->trace[in], s->trace[in ^ 1], st);
+    if (rc) return rc;
+  }
+  const int in = (par + 4) & 1;
+  for (int c = 0; c < kHostChunks; ++c) {
+    if (tb[c] == tb[c + 1]) continue;
+    rc = launch_stage(s, 1, 4, dt, q_dev, res_dev, nullptr, s->trace[in], s->trace[in ^ 1], st,
+                      tb[c], tb[c + 1]);
+    if (rc) return rc;
+    BB_CUDA(s->ctx, cudaEventRecord(ev[1 + kHostChunks + c], st));
+    BB_CUDA(s->ctx, cudaStreamWaitEvent(cs, ev[1 + kHostChunks + c], 0));
+    for (int f = 0; f < s->nf; ++f) {
+      const size_t off = ((size_t)f * s->K + eb[c]) * row;
+      BB_CUDA(s->ctx, cudaMemcpyAsync(hout + off, qd + off, (eb[c + 1] - eb[c]) * row,
+                                      cudaMemcpyDeviceToHost, cs));
+    }
+  }
+  BB_CUDA(s->ctx, cudaEventRecord(ev[1 + 2 * kHostChunks], cs));
+  BB_CUDA(s->ctx, cudaStreamWaitEvent(st, ev[1 + 2 * kHostChunks], 0));
   return BB_OK;
 }

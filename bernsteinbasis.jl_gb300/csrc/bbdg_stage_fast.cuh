@@ -7,6 +7,7 @@ struct FastStageParams {
   const uint32_t* gtab;  // degree tables (DegTables::d_words) and their word offsets
   int o_node3, o_node3m1, o_fvol, o_fperm, o_sslot;
   int64_t K;
+  int64_t tile_begin, tile_end;  // tiles [tile_begin, tile_end) of EPB elements (end 0 = all)
   int mode;              // 0: rhs only, 1: LSRK stage update
   float rkA, rkB, dt, tau;
   float* q;              // [NF][K][Np]

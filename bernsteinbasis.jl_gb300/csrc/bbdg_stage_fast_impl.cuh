@@ -249,7 +249,8 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
   __shared__ int s_fail;
   const int tid = threadIdx.x;
   const int64_t K = P.K;
-  const int64_t ntiles = K / EPB;  // the host guarantees K % EPB == 0
+  // this launch's tiles end at ntiles (the host guarantees K % EPB == 0)
+  const int64_t ntiles = P.tile_end > 0 ? P.tile_end : K / EPB;
   const uint32_t wlim = P.wait_iters ? P.wait_iters : (1u << 24);
   const bool stage = P.mode != 0;
   // element threads: element le, lane u within the element
@@ -380,7 +381,7 @@ __global__ void __launch_bounds__(FastLayout<N, PHYS, EPB, TPE>::NT,
   __syncthreads();
   // the first two tiles of this block go to the two slots; the first chain thread issues
   // every bulk copy and counts them per barrier (for the drain at the end)
-  const int64_t t0 = blockIdx.x;
+  const int64_t t0 = P.tile_begin + blockIdx.x;
   const bool issuer = tid == NTE;
   uint32_t iss0 = 0u, iss1 = 0u, iss2 = 0u;
   if (issuer && t0 < ntiles) {
@@ -878,7 +879,9 @@ int launch_fast_t(const FastLaunch& fl, const FastStageParams& P0, cudaStream_t 
       per_sm < 1)
     return BB_ERR_CUDA;
   if (P.K % EPB != 0) return BB_ERR_ARG;
-  const int64_t ntiles = P.K / EPB;
+  const int64_t tend = P.tile_end > 0 ? P.tile_end : P.K / EPB;
+  if (P.tile_begin < 0 || P.tile_begin >= tend || tend > P.K / EPB) return BB_ERR_ARG;
+  const int64_t ntiles = tend - P.tile_begin;
   int64_t grid = (int64_t)per_sm * fl.num_sms;
   if (grid > ntiles) grid = ntiles;
   kern<<<(int)grid, L::NT, L::BYTES, st>>>(P);

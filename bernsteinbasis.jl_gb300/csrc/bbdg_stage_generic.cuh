@@ -58,6 +58,7 @@ struct StageParams {
   DegTables tab;
   const uint32_t* gtab;
   int64_t K;
+  int64_t tile_begin, tile_end;  // stage_kernel's tiles [tile_begin, tile_end) (end 0 = all)
   int epb;
   int mode;             // 0: write rhs to `rhs`; 1: LSRK stage update of q and res
   T rkA, rkB, dt, tau;  // stage coefficients, time step, penalty (tau <= 0: as written)
