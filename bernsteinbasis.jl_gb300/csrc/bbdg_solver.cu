@@ -77,7 +77,7 @@ struct bb_solver {
   int* d_status = nullptr;
   cudaStream_t cap_stream = nullptr;
   cudaStream_t copy_stream = nullptr;  // bb_lsrk_run_host's upload/download stream
-  cudaEvent_t copy_ev[2 * 4 + 2] = {};  // its events (4 = kHostChunks)
+  cudaEvent_t copy_ev[2 * 8 + 2] = {};  // its events (8 = kHostChunks)
   // graph cache: one graph per starting trace buffer parity
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   void* g_q = nullptr;
@@ -509,7 +509,7 @@ int run_steps(bb_solver* s, double dt, int nsteps, void* q, void* res, int use_g
 }
 
 // The host-buffer path's second stream and its events, made on first use.
-constexpr int kHostChunks = 4;
+constexpr int kHostChunks = 8;
 static_assert(sizeof(bb_solver::copy_ev) / sizeof(cudaEvent_t) == 2 * kHostChunks + 2,
               "one start, kHostChunks upload, kHostChunks compute and one done event");
 int ensure_copy_stream(bb_solver* s) {

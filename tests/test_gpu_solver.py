@@ -115,7 +115,7 @@ def test_pipelined_host_path_equals_the_device_path(cuda, bb, case, nsteps):
     """bb_lsrk_run_host uploads the state in element ranges (traces extracted per range) and
     splits the last stage into ranges whose downloads overlap the later ranges' compute; the
     result equals the device-resident run bitwise, with and without the step graph, for the
-    specialised and the generic kernels (81 tiles: ranges of 20 and 21 tiles)."""
+    specialised and the generic kernels (81 tiles: ranges of 10 and 11 tiles)."""
     import torch
     physics, N, dt_name = case
     m = bb.uniform_tet_mesh(3)
