@@ -125,7 +125,7 @@ const DegTables* bb_tables(bb_ctx* ctx, int N);
 // The context's device error word (allocated on first use; nullptr on failure).
 int* bb_ctx_status_word(bb_ctx* ctx);
 // Degree-specialised FP32 lift (bbdg_lift_fast.cu): nfaces 4 or 1; -1 when N has none.
-// Degree-specialised FP32 derivatives (bbdg_deriv_fast.cu, N <= 11): mask 1, 2, 4 or 7; -1 when
+// Degree-specialised FP32 derivatives (bbdg_deriv_fast.cu, N <= 15): mask 1, 2, 4 or 7; -1 when
 // none applies.
 int bb_deriv_fast(bb_ctx* ctx, const DegTables* t, int64_t K, int mask, const void* x, void* o0,
                   void* o1, void* o2, cudaStream_t st);

@@ -68,16 +68,18 @@ def test_lift_matches_oracle(cuda, bb, oracle_cpu, N, dt, K):
     assert rel(of.cpu().numpy(), want) < TOL[dt]
 
 
-@pytest.mark.parametrize("N", [1, 4, 8, 9, 10, 12])
+@pytest.mark.parametrize("N", range(1, 16))
 def test_deriv_fp32_many_tiles_and_misaligned(cuda, bb, oracle_cpu, N):
-    """K = 20011 gives more tiles than the one-warp blocks of the degree-specialised FP32
-    derivative kernel, and a ragged last tile whose inputs end inside a float4 for odd Np; a
-    sample of columns is checked against the oracle for each axis, the fused gradient equals
-    the single-axis results bitwise, and misaligned columns (the generic kernel) agree."""
+    """About 12 M inputs give more tiles than the grid of the degree-specialised FP32
+    derivative kernel has blocks at every degree (each degree has its own block shape and
+    tile), so blocks alternate between their two shared buffers; K is odd, so for odd Np the
+    last tile is ragged and its inputs end inside a float4. A sample of columns is checked
+    against the oracle for each axis, the fused gradient equals the single-axis results
+    bitwise, and misaligned columns (the generic kernel) agree."""
     import torch
     rng = np.random.default_rng(110 + N)
-    K = 20011
     Np = bb.np3(N)
+    K = max(20011, (12_000_000 // Np) | 1)
     x = rng.uniform(-1, 1, (K, Np)).astype(np.float32)
     xd = torch.tensor(x, device=cuda)
     cols = np.r_[0:30, K // 2:K // 2 + 30, K - 30:K]
