@@ -253,6 +253,7 @@ int launch_fast_lane(bb_batch* b, int p, int s, int par, cudaStream_t st) {
   P.status = b->d_status;
   FastLaunch fl;
   fl.num_sms = b->ctx->num_sms;
+  fl.device = b->ctx->device;
   fl.wait_iters = b->ctx->wait_iters;
   fl.fault = b->ctx->test_fault;
   const int rc = bb_fast_launch(b->fast[p], fl, P, st);

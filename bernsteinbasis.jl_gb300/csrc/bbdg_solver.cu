@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "bbdg_internal.cuh"
 #include "bbdg_stage_fast.cuh"
@@ -59,6 +60,25 @@ const double kRK4B[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13
 // -------------------------------------------------------------------------------------
 // solver object
 // -------------------------------------------------------------------------------------
+// bb_lsrk_run_host's schedule: the elements split into C ranges of whole tiles ("chunks"),
+// uploaded in breadth-first order over the chunk neighbour graph; each LSRK stage runs chunk
+// by chunk on its own stream, a chunk as soon as the previous stage has finished on every
+// chunk that holds one of its elements' neighbours.
+struct HostPlan {
+  int epb = 0, C = 0;
+  std::vector<int64_t> tb, eb;  // chunk c: tiles [tb[c], tb[c+1]), elements [eb[c], eb[c+1])
+  std::vector<int> up;          // chunks in upload order
+  std::vector<int> order[5];    // chunks in launch order, per stage
+  std::vector<int> ready0;      // order[0][i] may run once uploads 0..ready0[i] are in
+  std::vector<int> wait[5];     // order[s][i] (s >= 1) waits for launch wait[s][i] of stage s-1
+  std::vector<cudaEvent_t> ev;  // 5 C stage launches, C uploads, start, middle, done
+  cudaEvent_t& stage_ev(int s, int i) { return ev[(size_t)s * C + i]; }
+  cudaEvent_t& up_ev(int p) { return ev[(size_t)5 * C + p]; }
+  cudaEvent_t& start_ev() { return ev[(size_t)6 * C]; }
+  cudaEvent_t& mid_ev() { return ev[(size_t)6 * C + 1]; }
+  cudaEvent_t& done_ev() { return ev[(size_t)6 * C + 2]; }
+};
+
 struct bb_solver {
   bb_ctx* ctx = nullptr;
   int physics = 0, N = 0, dtype = 0, nf = 0;
@@ -76,8 +96,11 @@ struct bb_solver {
   size_t trace_bytes = 0;
   int* d_status = nullptr;
   cudaStream_t cap_stream = nullptr;
-  cudaStream_t copy_stream = nullptr;  // bb_lsrk_run_host's upload/download stream
-  cudaEvent_t copy_ev[2 * 8 + 2] = {};  // its events (8 = kHostChunks)
+  // bb_lsrk_run_host: upload and download streams, one stream per LSRK stage, the schedule
+  cudaStream_t copy_stream = nullptr;
+  cudaStream_t down_stream = nullptr;
+  cudaStream_t stage_stream[5] = {};
+  HostPlan* plan = nullptr;
   // graph cache: one graph per starting trace buffer parity
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   void* g_q = nullptr;
@@ -178,6 +201,7 @@ int launch_fast(bb_solver* s, int mode, int stage, double dt, void* q, void* res
   P.status = s->d_status;
   FastLaunch fl;
   fl.num_sms = s->ctx->num_sms;
+  fl.device = s->ctx->device;
   fl.wait_iters = s->ctx->wait_iters;
   fl.fault = s->ctx->test_fault;
   const int rc = bb_fast_launch(s->fast, fl, P, st);
@@ -380,8 +404,14 @@ extern "C" int bb_solver_destroy(bb_solver* s) {
   cudaFree(s->d_status);
   if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
   if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
-  for (auto& e : s->copy_ev)
-    if (e) cudaEventDestroy(e);
+  if (s->down_stream) cudaStreamDestroy(s->down_stream);
+  for (auto& x : s->stage_stream)
+    if (x) cudaStreamDestroy(x);
+  if (s->plan) {
+    for (auto& e : s->plan->ev)
+      if (e) cudaEventDestroy(e);
+    delete s->plan;
+  }
   delete s;
   return BB_OK;
 }
@@ -477,9 +507,9 @@ extern "C" int bb_solver_check(bb_solver* s, void* stream) {
 
 namespace {
 
-// nsteps LSRK steps from traces of q already current in trace buffer 0.
+// nsteps LSRK steps from traces of q already current in trace buffer par0.
 int run_steps(bb_solver* s, double dt, int nsteps, void* q, void* res, int use_graph,
-              cudaStream_t st) {
+              cudaStream_t st, int par0 = 0) {
   int rc = BB_OK;
   if (use_graph) {
     if (s->g_q != q || s->g_res != res || s->g_dt != dt || s->g_epb != s->epb ||
@@ -496,31 +526,231 @@ int run_steps(bb_solver* s, double dt, int nsteps, void* q, void* res, int use_g
     s->g_epb = s->epb;
     s->g_epoch = s->ctx->config_epoch;
     for (int step = 0; step < nsteps; ++step) {
-      BB_CUDA(s->ctx, cudaGraphLaunch(s->graph[step & 1], st));
+      BB_CUDA(s->ctx, cudaGraphLaunch(s->graph[(par0 + step) & 1], st));
       s->ctx->launches += 5;
     }
   } else {
     for (int step = 0; step < nsteps; ++step) {
-      rc = enqueue_step(s, dt, q, res, step & 1, st);
+      rc = enqueue_step(s, dt, q, res, (par0 + step) & 1, st);
       if (rc) return rc;
     }
   }
   return BB_OK;
 }
 
-// The host-buffer path's second stream and its events, made on first use.
-constexpr int kHostChunks = 8;
-static_assert(sizeof(bb_solver::copy_ev) / sizeof(cudaEvent_t) == 2 * kHostChunks + 2,
-              "one start, kHostChunks upload, kHostChunks compute and one done event");
-int ensure_copy_stream(bb_solver* s) {
-  if (s->copy_stream) return BB_OK;
-  for (auto& e : s->copy_ev)
-    if (!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
-      return bb_fail(s->ctx, BB_ERR_CUDA, "copy event creation failed");
-  cudaStream_t cs = nullptr;
-  if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
-    return bb_fail(s->ctx, BB_ERR_CUDA, "copy stream creation failed");
-  s->copy_stream = cs;
+// bb_lsrk_run_host's streams, made on first use.
+int ensure_host_streams(bb_solver* s) {
+  cudaStream_t* all[7] = {&s->copy_stream, &s->down_stream, &s->stage_stream[0],
+                          &s->stage_stream[1], &s->stage_stream[2], &s->stage_stream[3],
+                          &s->stage_stream[4]};
+  for (cudaStream_t* x : all)
+    if (!*x && cudaStreamCreateWithFlags(x, cudaStreamNonBlocking) != cudaSuccess)
+      return bb_fail(s->ctx, BB_ERR_CUDA, "stream creation failed");
+  return BB_OK;
+}
+
+// Builds bb_lsrk_run_host's schedule for the solver's tile size (see HostPlan). The chunk
+// neighbour graph comes from one download of the connectivity; entries that name no element
+// (the kernels report those) add no edge.
+int build_host_plan(bb_solver* s) {
+  if (s->plan && s->plan->epb == s->epb) return BB_OK;
+  if (s->plan) {
+    for (auto& e : s->plan->ev)
+      if (e) cudaEventDestroy(e);
+    delete s->plan;
+    s->plan = nullptr;
+  }
+  HostPlan* P = new (std::nothrow) HostPlan();
+  if (!P) return BB_ERR_NOMEM;
+  const int64_t K = s->K;
+  const int64_t ntiles = (K + s->epb - 1) / s->epb;
+  // up to 24 chunks of at least 8 tiles
+  const int C = (int)std::min<int64_t>(24, std::max<int64_t>(1, ntiles / 8));
+  P->epb = s->epb;
+  P->C = C;
+  P->tb.resize(C + 1);
+  P->eb.resize(C + 1);
+  for (int c = 0; c <= C; ++c) {
+    P->tb[c] = ntiles * c / C;
+    P->eb[c] = std::min<int64_t>(K, P->tb[c] * s->epb);
+  }
+  std::vector<int32_t> conn((size_t)K * 4);
+  if (cudaMemcpy(conn.data(), s->conn, conn.size() * sizeof(int32_t), cudaMemcpyDefault) !=
+      cudaSuccess) {
+    delete P;
+    return bb_fail(s->ctx, BB_ERR_CUDA, "connectivity download failed");
+  }
+  std::vector<uint64_t> nb(C, 0);  // neighbour chunks of each chunk (itself included)
+  for (int c = 0; c < C; ++c) {
+    nb[c] |= uint64_t(1) << c;
+    for (int64_t e = P->eb[c]; e < P->eb[c + 1]; ++e)
+      for (int f = 0; f < 4; ++f) {
+        const int64_t n = conn[(size_t)e * 4 + f] >> 5;
+        if (n < 0 || n >= K) continue;
+        const int cn = (int)(std::upper_bound(P->eb.begin(), P->eb.end(), n) - P->eb.begin()) - 1;
+        nb[c] |= uint64_t(1) << cn;
+        nb[cn] |= uint64_t(1) << c;
+      }
+  }
+  // upload order: breadth-first from chunk 0, lower chunks first
+  std::vector<int> pos(C, -1);
+  for (int root = 0; root < C; ++root) {
+    if (pos[root] >= 0) continue;
+    size_t head = P->up.size();
+    pos[root] = (int)P->up.size();
+    P->up.push_back(root);
+    while (head < P->up.size()) {
+      const int c = P->up[head++];
+      for (int d = 0; d < C; ++d)
+        if ((nb[c] >> d & 1) && pos[d] < 0) {
+          pos[d] = (int)P->up.size();
+          P->up.push_back(d);
+        }
+    }
+  }
+  // stage 0 (of a step fed by the uploads): a chunk may run once every neighbour chunk is in
+  std::vector<int> key(C), idx(C);
+  auto sort_by = [&](std::vector<int>& order, const std::vector<int>& tie) {
+    order.resize(C);
+    for (int c = 0; c < C; ++c) order[c] = c;
+    std::sort(order.begin(), order.end(), [&](int a, int b) {
+      return key[a] != key[b] ? key[a] < key[b] : tie[a] < tie[b];
+    });
+  };
+  for (int c = 0; c < C; ++c) {
+    key[c] = 0;
+    for (int d = 0; d < C; ++d)
+      if (nb[c] >> d & 1) key[c] = std::max(key[c], pos[d]);
+  }
+  sort_by(P->order[0], pos);
+  P->ready0.resize(C);
+  for (int i = 0; i < C; ++i) P->ready0[i] = key[P->order[0][i]];
+  for (int st = 1; st < 5; ++st) {
+    for (int i = 0; i < C; ++i) idx[P->order[st - 1][i]] = i;
+    for (int c = 0; c < C; ++c) {
+      key[c] = 0;
+      for (int d = 0; d < C; ++d)
+        if (nb[c] >> d & 1) key[c] = std::max(key[c], idx[d]);
+    }
+    sort_by(P->order[st], idx);
+    P->wait[st].resize(C);
+    for (int i = 0; i < C; ++i) P->wait[st][i] = key[P->order[st][i]];
+  }
+  P->ev.assign((size_t)6 * C + 3, nullptr);
+  for (auto& e : P->ev)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      for (auto& x : P->ev)
+        if (x) cudaEventDestroy(x);
+      delete P;
+      return bb_fail(s->ctx, BB_ERR_CUDA, "event creation failed");
+    }
+  s->plan = P;
+  return BB_OK;
+}
+
+// Copies field slices of elements [e0, e1) between the device state and a host buffer.
+int copy_range(bb_solver* s, char* dst, const char* src, int64_t e0, int64_t e1,
+               cudaMemcpyKind kind, cudaStream_t st) {
+  const size_t row = (size_t)s->tab->Np * dtype_size(s->dtype);
+  for (int f = 0; f < s->nf; ++f) {
+    const size_t off = ((size_t)f * s->K + e0) * row;
+    BB_CUDA(s->ctx, cudaMemcpyAsync(dst + off, src + off, (size_t)(e1 - e0) * row, kind, st));
+  }
+  return BB_OK;
+}
+
+// One LSRK step chunk by chunk on the stage streams (HostPlan). par: the trace buffer the step
+// starts from. upload: the chunks are first uploaded (copy_stream), and each one's traces are
+// extracted as it lands; otherwise the traces are current and stage 0 is free to run.
+// download: each chunk goes to hout as soon as its last stage is done.
+//
+// Every item (an upload, an extraction, a stage launch, a download) gets a level one above
+// that of the item it waits for and of its predecessor on its stream, and the items are
+// enqueued by level: CUDA maps streams onto a few hardware queues, and streams that share one
+// then see the items in about the order they can run instead of stage after stage.
+int host_plan_step(bb_solver* s, double dt, void* q, void* res, int par, bool upload,
+                   bool download, const char* hin, char* hout) {
+  HostPlan& P = *s->plan;
+  const int C = P.C;
+  enum { UP, EXTRACT, STAGE, DOWN };
+  struct Item {
+    int level, stream, seq, kind, stage, i;
+  };
+  std::vector<Item> items;
+  items.reserve((size_t)8 * C);
+  // streams: 0 uploads, 1..5 stages 0..4, 6 downloads
+  std::vector<int> lv_up(C), lv_stage((size_t)5 * C);
+  int seq = 0, last = -1;
+  if (upload)
+    for (int p = 0; p < C; ++p) {
+      lv_up[p] = p;
+      items.push_back({p, 0, seq++, UP, 0, p});
+    }
+  int i = 0;
+  last = -1;
+  for (int p = 0; p < C; ++p) {
+    if (upload) {
+      last = std::max(last + 1, lv_up[p] + 1);
+      items.push_back({last, 1, seq++, EXTRACT, 0, p});
+    }
+    for (; i < C && (!upload || P.ready0[i] <= p); ++i) {
+      last = last + 1;
+      lv_stage[i] = last;
+      items.push_back({last, 1, seq++, STAGE, 0, i});
+    }
+  }
+  for (int st = 1; st < 5; ++st) {
+    last = -1;
+    for (int j = 0; j < C; ++j) {
+      last = std::max(last + 1, lv_stage[(size_t)(st - 1) * C + P.wait[st][j]] + 1);
+      lv_stage[(size_t)st * C + j] = last;
+      items.push_back({last, 1 + st, seq++, STAGE, st, j});
+    }
+  }
+  if (download) {
+    last = -1;
+    for (int j = 0; j < C; ++j) {
+      last = std::max(last + 1, lv_stage[(size_t)4 * C + j] + 1);
+      items.push_back({last, 6, seq++, DOWN, 4, j});
+    }
+  }
+  std::sort(items.begin(), items.end(), [](const Item& a, const Item& b) {
+    return a.level != b.level ? a.level < b.level
+                              : a.stream != b.stream ? a.stream < b.stream : a.seq < b.seq;
+  });
+  cudaStream_t* ss = s->stage_stream;
+  int waited[5] = {-1, -1, -1, -1, -1};
+  for (const Item& it : items) {
+    int rc = BB_OK;
+    if (it.kind == UP) {
+      const int c = P.up[it.i];
+      rc = copy_range(s, static_cast<char*>(q), hin, P.eb[c], P.eb[c + 1], cudaMemcpyHostToDevice,
+                      s->copy_stream);
+      if (rc) return rc;
+      BB_CUDA(s->ctx, cudaEventRecord(P.up_ev(it.i), s->copy_stream));
+    } else if (it.kind == EXTRACT) {
+      const int c = P.up[it.i];
+      BB_CUDA(s->ctx, cudaStreamWaitEvent(ss[0], P.up_ev(it.i), 0));
+      rc = launch_extract(s, q, s->trace[par], ss[0], P.eb[c], P.eb[c + 1]);
+    } else if (it.kind == STAGE) {
+      const int st = it.stage, c = P.order[st][it.i];
+      if (st > 0 && P.wait[st][it.i] != waited[st]) {
+        waited[st] = P.wait[st][it.i];
+        BB_CUDA(s->ctx, cudaStreamWaitEvent(ss[st], P.stage_ev(st - 1, waited[st]), 0));
+      }
+      const int in = (par + st) & 1;
+      rc = launch_stage(s, 1, st, dt, q, res, nullptr, s->trace[in], s->trace[in ^ 1], ss[st],
+                        P.tb[c], P.tb[c + 1]);
+      if (rc) return rc;
+      BB_CUDA(s->ctx, cudaEventRecord(P.stage_ev(st, it.i), ss[st]));
+    } else {
+      const int c = P.order[4][it.i];
+      BB_CUDA(s->ctx, cudaStreamWaitEvent(s->down_stream, P.stage_ev(4, it.i), 0));
+      rc = copy_range(s, hout, static_cast<const char*>(q), P.eb[c], P.eb[c + 1],
+                      cudaMemcpyDeviceToHost, s->down_stream);
+    }
+    if (rc) return rc;
+  }
   return BB_OK;
 }
 
@@ -541,11 +771,13 @@ extern "C" int bb_lsrk_run(bb_solver* s, double dt, int nsteps, void* q, void* r
   return run_steps(s, dt, nsteps, q, res, use_graph, st);
 }
 
-// Host state in and out, pipelined: the state goes up in kHostChunks element ranges on a
-// second stream, and each range's traces are extracted as soon as it has landed; the steps
-// run as in bb_lsrk_run except the last stage of the last step, which runs range by range so
-// that each range's download starts while the later ranges are still being computed. The
-// caller's stream waits for the last download, so the call stays stream-ordered.
+// Host state in and out, pipelined over element chunks (HostPlan): the uploads, each LSRK
+// stage and the downloads run on their own streams, ordered by events only where the mesh
+// couples the chunks, so the two copy directions overlap each other and the compute. With
+// several steps the first runs chunk by chunk behind the uploads, the middle ones as whole
+// launches (or the step graphs) on the caller's stream, and the last chunk by chunk ahead of
+// the downloads. The caller's stream waits for the last download, so the call stays
+// stream-ordered.
 extern "C" int bb_lsrk_run_host(bb_solver* s, double dt, int nsteps, const void* q_host_in,
                                 void* q_host_out, void* q_dev, void* res_dev, int use_graph,
                                 void* stream) {
@@ -556,67 +788,38 @@ extern "C" int bb_lsrk_run_host(bb_solver* s, double dt, int nsteps, const void*
   int rc = bb_set_device(s->ctx);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
-  const size_t esz = dtype_size(s->dtype);
-  const size_t row = (size_t)s->tab->Np * esz;  // one element of one field
-  const size_t bytes = (size_t)s->nf * s->K * row;
+  const size_t bytes = (size_t)s->nf * s->K * s->tab->Np * dtype_size(s->dtype);
   if (nsteps == 0) {
     BB_CUDA(s->ctx, cudaMemcpyAsync(q_dev, q_host_in, bytes, cudaMemcpyHostToDevice, st));
     BB_CUDA(s->ctx, cudaMemcpyAsync(q_host_out, q_dev, bytes, cudaMemcpyDeviceToHost, st));
     return BB_OK;
   }
-  rc = ensure_copy_stream(s);
+  rc = ensure_host_streams(s);
   if (rc) return rc;
-  cudaStream_t cs = s->copy_stream;
-  cudaEvent_t* ev = s->copy_ev;  // [0] start, [1..C] uploaded, [C+1..2C] computed, [2C+1] done
-  // ranges of whole tiles (the specialised kernels need them); empty ranges are skipped
-  const int64_t ntiles = (s->K + s->epb - 1) / s->epb;
-  int64_t tb[kHostChunks + 1], eb[kHostChunks + 1];
-  for (int c = 0; c <= kHostChunks; ++c) {
-    tb[c] = ntiles * c / kHostChunks;
-    eb[c] = std::min<int64_t>(s->K, tb[c] * s->epb);
-  }
-  char* qd = static_cast<char*>(q_dev);
-  const char* hin = static_cast<const char*>(q_host_in);
+  rc = build_host_plan(s);
+  if (rc) return rc;
+  HostPlan& P = *s->plan;
   char* hout = static_cast<char*>(q_host_out);
-  BB_CUDA(s->ctx, cudaEventRecord(ev[0], st));
-  BB_CUDA(s->ctx, cudaStreamWaitEvent(cs, ev[0], 0));
-  for (int c = 0; c < kHostChunks; ++c) {
-    if (eb[c] == eb[c + 1]) continue;
-    for (int f = 0; f < s->nf; ++f) {
-      const size_t off = ((size_t)f * s->K + eb[c]) * row;
-      BB_CUDA(s->ctx, cudaMemcpyAsync(qd + off, hin + off, (eb[c + 1] - eb[c]) * row,
-                                      cudaMemcpyHostToDevice, cs));
-    }
-    BB_CUDA(s->ctx, cudaEventRecord(ev[1 + c], cs));
-    BB_CUDA(s->ctx, cudaStreamWaitEvent(st, ev[1 + c], 0));
-    rc = launch_extract(s, q_dev, s->trace[0], st, eb[c], eb[c + 1]);
-    if (rc) return rc;
-  }
+  // every stream starts after the caller's earlier work
+  BB_CUDA(s->ctx, cudaEventRecord(P.start_ev(), st));
+  BB_CUDA(s->ctx, cudaStreamWaitEvent(s->copy_stream, P.start_ev(), 0));
+  BB_CUDA(s->ctx, cudaStreamWaitEvent(s->down_stream, P.start_ev(), 0));
+  for (cudaStream_t x : s->stage_stream) BB_CUDA(s->ctx, cudaStreamWaitEvent(x, P.start_ev(), 0));
+  rc = host_plan_step(s, dt, q_dev, res_dev, 0, true, nsteps == 1,
+                      static_cast<const char*>(q_host_in), hout);
+  if (rc) return rc;
   if (nsteps > 1) {
-    rc = run_steps(s, dt, nsteps - 1, q_dev, res_dev, use_graph, st);
+    // the middle steps on the caller's stream once the first step is done everywhere
+    BB_CUDA(s->ctx, cudaEventRecord(P.mid_ev(), s->stage_stream[4]));
+    BB_CUDA(s->ctx, cudaStreamWaitEvent(st, P.mid_ev(), 0));
+    rc = run_steps(s, dt, nsteps - 2, q_dev, res_dev, use_graph, st, 1);
+    if (rc) return rc;
+    BB_CUDA(s->ctx, cudaEventRecord(P.mid_ev(), st));
+    for (cudaStream_t x : s->stage_stream) BB_CUDA(s->ctx, cudaStreamWaitEvent(x, P.mid_ev(), 0));
+    rc = host_plan_step(s, dt, q_dev, res_dev, (nsteps - 1) & 1, false, true, nullptr, hout);
     if (rc) return rc;
   }
-  const int par = (nsteps - 1) & 1;
-  for (int stage = 0; stage < 4; ++stage) {
-    const int in = (par + stage) & 1;
-    rc = launch_stage(s, 1, stage, dt, q_dev, res_dev, nullptr, s->trace[in], s->trace[in ^ 1], st);
-    if (rc) return rc;
-  }
-  const int in = (par + 4) & 1;
-  for (int c = 0; c < kHostChunks; ++c) {
-    if (tb[c] == tb[c + 1]) continue;
-    rc = launch_stage(s, 1, 4, dt, q_dev, res_dev, nullptr, s->trace[in], s->trace[in ^ 1], st,
-                      tb[c], tb[c + 1]);
-    if (rc) return rc;
-    BB_CUDA(s->ctx, cudaEventRecord(ev[1 + kHostChunks + c], st));
-    BB_CUDA(s->ctx, cudaStreamWaitEvent(cs, ev[1 + kHostChunks + c], 0));
-    for (int f = 0; f < s->nf; ++f) {
-      const size_t off = ((size_t)f * s->K + eb[c]) * row;
-      BB_CUDA(s->ctx, cudaMemcpyAsync(hout + off, qd + off, (eb[c + 1] - eb[c]) * row,
-                                      cudaMemcpyDeviceToHost, cs));
-    }
-  }
-  BB_CUDA(s->ctx, cudaEventRecord(ev[1 + 2 * kHostChunks], cs));
-  BB_CUDA(s->ctx, cudaStreamWaitEvent(st, ev[1 + 2 * kHostChunks], 0));
+  BB_CUDA(s->ctx, cudaEventRecord(P.done_ev(), s->down_stream));
+  BB_CUDA(s->ctx, cudaStreamWaitEvent(st, P.done_ev(), 0));
   return BB_OK;
 }

@@ -28,6 +28,7 @@ struct FastStageParams {
 
 struct FastLaunch {
   int num_sms;
+  int device;           // CUDA device ordinal (the per-device launch set-up is cached)
   uint32_t wait_iters;  // copied into FastStageParams (the context's wait limit)
   int fault;            // copied into FastStageParams (the context's test-only fault mode)
 };

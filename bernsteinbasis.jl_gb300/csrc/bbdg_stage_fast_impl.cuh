@@ -31,6 +31,7 @@
 // mbarrier completion, bounded waits) while tiles i and i+1 are being worked on.
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
 #include <vector>
 
@@ -870,14 +871,20 @@ int launch_fast_t(const FastLaunch& fl, const FastStageParams& P0, cudaStream_t 
   for (int g = 0; g < 16; ++g) P.vstart[g] = vg.start[g], P.vlen[g] = vg.len[g];
   P.wait_iters = fl.wait_iters;
   P.fault = fl.fault;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES) !=
-      cudaSuccess)
-    return BB_ERR_CUDA;
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, L::NT, L::BYTES) !=
-          cudaSuccess ||
-      per_sm < 1)
-    return BB_ERR_CUDA;
+  // shared-memory opt-in and resident blocks per SM, set up once per device (the host-buffer
+  // path launches each stage in up to 24 tile ranges)
+  static std::atomic<int> per_sm_of[64];
+  int per_sm = fl.device >= 0 && fl.device < 64 ? per_sm_of[fl.device].load() : 0;
+  if (per_sm < 1) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES) !=
+        cudaSuccess)
+      return BB_ERR_CUDA;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, L::NT, L::BYTES) !=
+            cudaSuccess ||
+        per_sm < 1)
+      return BB_ERR_CUDA;
+    if (fl.device >= 0 && fl.device < 64) per_sm_of[fl.device].store(per_sm);
+  }
   if (P.K % EPB != 0) return BB_ERR_ARG;
   const int64_t tend = P.tile_end > 0 ? P.tile_end : P.K / EPB;
   if (P.tile_begin < 0 || P.tile_begin >= tend || tend > P.K / EPB) return BB_ERR_ARG;

@@ -147,11 +147,14 @@ int bb_lsrk_run(bb_solver* s, double dt, int nsteps, void* q, void* res, int use
 int bb_solver_check(bb_solver* s, void* stream);
 
 /* The same with host state: copies q_host_in to q_dev, advances, copies back to
- * q_host_out. Pipelined: the state goes up in element ranges on a solver-owned second stream
- * (each range's traces are extracted as it lands) and the last stage runs range by range, each
- * range going down while the later ones compute; the results are those of bb_lsrk_run. The
- * call is stream-ordered: `stream` waits for the last download. The host buffers must stay
- * valid until then; pinned host memory is needed for the copies to overlap. q_host_in and
+ * q_host_out. Pipelined over up to 24 element ranges ("chunks") on solver-owned streams: one
+ * for the uploads, one per LSRK stage, one for the downloads. A chunk's traces are extracted
+ * as it lands, each stage runs on a chunk once the previous stage has finished on the chunks
+ * holding its neighbours (read once from conn), and a chunk goes down as soon as its last
+ * stage is done, so both copy directions overlap the compute; with several steps the middle
+ * ones run as whole launches on `stream`. The results are those of bb_lsrk_run. The call is
+ * stream-ordered: `stream` waits for the last download. The host buffers must stay valid
+ * until then; pinned host memory is needed for the copies to overlap. q_host_in and
  * q_host_out may be the same buffer. */
 int bb_lsrk_run_host(bb_solver* s, double dt, int nsteps, const void* q_host_in,
                      void* q_host_out, void* q_dev, void* res_dev, int use_graph,

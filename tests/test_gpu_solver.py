@@ -112,10 +112,11 @@ def test_graph_and_stream_paths_agree(cuda, bb):
 @pytest.mark.parametrize("nsteps", [1, 2, 3])
 @pytest.mark.parametrize("case", [("wave", 5, "f32"), ("maxwell", 9, "f32"), ("wave", 3, "f64")])
 def test_pipelined_host_path_equals_the_device_path(cuda, bb, case, nsteps):
-    """bb_lsrk_run_host uploads the state in element ranges (traces extracted per range) and
-    splits the last stage into ranges whose downloads overlap the later ranges' compute; the
-    result equals the device-resident run bitwise, with and without the step graph, for the
-    specialised and the generic kernels (81 tiles: ranges of 10 and 11 tiles)."""
+    """bb_lsrk_run_host runs the first and the last step chunk by chunk on one stream per
+    stage, ordered by the chunks' neighbours, behind the uploads and ahead of the downloads;
+    the result equals the device-resident run bitwise, with and without the step graph, for
+    the specialised and the generic kernels (81 tiles: 10 chunks of 8 or 9 tiles on the
+    periodic 3^3-hex mesh, whose chunk graph wraps around)."""
     import torch
     physics, N, dt_name = case
     m = bb.uniform_tet_mesh(3)
@@ -132,6 +133,31 @@ def test_pipelined_host_path_equals_the_device_path(cuda, bb, case, nsteps):
         s.run_host(hin, hout, qd, rd, step, nsteps, graph=graph)
         torch.cuda.synchronize()
         assert torch.equal(hout, qa.cpu()) and torch.equal(rd, ra) and torch.equal(qd, qa)
+    s.check()
+
+
+@pytest.mark.parametrize("nsteps", [1, 3])
+def test_host_path_24_chunks_on_the_headline_tile(cuda, bb, nsteps):
+    """8^3 hexes x 6 tets (K = 3072) on the 4-element x 288-thread wave tile: 768 tiles in 24
+    chunks of 32, five stage streams; bitwise equal to the device-resident run."""
+    import torch
+    m = bb.uniform_tet_mesh(8)
+    s = bb.DGSolver(m, 9, "wave", dtype=torch.float32, tau=1.0)
+    s.set_kernel("specialised")
+    s.set_tile(4, 288)
+    assert s.kernel == "specialised"
+    rng = np.random.default_rng(77 + nsteps)
+    q0 = torch.tensor(random_state(rng, s.nf, m.K, s.Np) * 1e-2, dtype=torch.float32, device=cuda)
+    step = s.dt_cfl()
+    qa, ra = q0.clone(), torch.zeros_like(q0)
+    s.run(qa, ra, step, nsteps)
+    hin = q0.cpu().pin_memory()
+    hout = torch.full_like(hin, float("nan")).pin_memory()
+    qd, rd = torch.empty_like(q0), torch.zeros_like(q0)
+    for _ in range(2):  # the second call reuses the schedule and its events
+        s.run_host(hin, hout, qd, rd, step, nsteps)
+        torch.cuda.synchronize()
+        assert torch.equal(hout, qa.cpu()) and torch.equal(qd, qa) and torch.equal(rd, ra)
     s.check()
 
 
