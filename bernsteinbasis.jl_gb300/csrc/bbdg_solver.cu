@@ -108,6 +108,15 @@ struct bb_solver {
   double g_dt = 0.0;
   int g_epb = 0;
   int64_t g_epoch = -1;  // the context's config_epoch the graphs were captured under
+  // bb_lsrk_run_host's one-step schedule as a graph, for the buffers and dt it was made with
+  cudaGraphExec_t host_graph = nullptr;
+  const void* hg_in = nullptr;
+  void* hg_out = nullptr;
+  void* hg_q = nullptr;
+  void* hg_res = nullptr;
+  double hg_dt = 0.0;
+  int hg_epb = 0;
+  int64_t hg_epoch = -1;
 };
 
 namespace {
@@ -284,6 +293,10 @@ void drop_graphs(bb_solver* s) {
       cudaGraphExecDestroy(g);
       g = nullptr;
     }
+  if (s->host_graph) {
+    cudaGraphExecDestroy(s->host_graph);
+    s->host_graph = nullptr;
+  }
 }
 
 // One LSRK step (5 stages) starting from trace buffer `par`; ends in buffer 1 - par.
@@ -771,13 +784,59 @@ extern "C" int bb_lsrk_run(bb_solver* s, double dt, int nsteps, void* q, void* r
   return run_steps(s, dt, nsteps, q, res, use_graph, st);
 }
 
+namespace {
+
+// Page-locked host memory (cudaHostAlloc / cudaHostRegister): copies from and to it can be
+// captured into a graph.
+bool pinned_host(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // the error of this query only
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+// Enqueues bb_lsrk_run_host's work (after the host plan and streams exist): every stream
+// starts after the caller's earlier work on st, and st waits for the last download.
+int enqueue_host_run(bb_solver* s, double dt, int nsteps, const void* q_host_in,
+                     void* q_host_out, void* q_dev, void* res_dev, int use_graph, cudaStream_t st) {
+  HostPlan& P = *s->plan;
+  char* hout = static_cast<char*>(q_host_out);
+  BB_CUDA(s->ctx, cudaEventRecord(P.start_ev(), st));
+  BB_CUDA(s->ctx, cudaStreamWaitEvent(s->copy_stream, P.start_ev(), 0));
+  BB_CUDA(s->ctx, cudaStreamWaitEvent(s->down_stream, P.start_ev(), 0));
+  for (cudaStream_t x : s->stage_stream) BB_CUDA(s->ctx, cudaStreamWaitEvent(x, P.start_ev(), 0));
+  int rc = host_plan_step(s, dt, q_dev, res_dev, 0, true, nsteps == 1,
+                          static_cast<const char*>(q_host_in), hout);
+  if (rc) return rc;
+  if (nsteps > 1) {
+    // the middle steps on the caller's stream once the first step is done everywhere
+    BB_CUDA(s->ctx, cudaEventRecord(P.mid_ev(), s->stage_stream[4]));
+    BB_CUDA(s->ctx, cudaStreamWaitEvent(st, P.mid_ev(), 0));
+    rc = run_steps(s, dt, nsteps - 2, q_dev, res_dev, use_graph, st, 1);
+    if (rc) return rc;
+    BB_CUDA(s->ctx, cudaEventRecord(P.mid_ev(), st));
+    for (cudaStream_t x : s->stage_stream) BB_CUDA(s->ctx, cudaStreamWaitEvent(x, P.mid_ev(), 0));
+    rc = host_plan_step(s, dt, q_dev, res_dev, (nsteps - 1) & 1, false, true, nullptr, hout);
+    if (rc) return rc;
+  }
+  BB_CUDA(s->ctx, cudaEventRecord(P.done_ev(), s->down_stream));
+  BB_CUDA(s->ctx, cudaStreamWaitEvent(st, P.done_ev(), 0));
+  return BB_OK;
+}
+
+}  // namespace
+
 // Host state in and out, pipelined over element chunks (HostPlan): the uploads, each LSRK
 // stage and the downloads run on their own streams, ordered by events only where the mesh
 // couples the chunks, so the two copy directions overlap each other and the compute. With
 // several steps the first runs chunk by chunk behind the uploads, the middle ones as whole
 // launches (or the step graphs) on the caller's stream, and the last chunk by chunk ahead of
-// the downloads. The caller's stream waits for the last download, so the call stays
-// stream-ordered.
+// the downloads. One step with use_graph set and pinned host buffers is captured once into a
+// graph (per host and device buffers and dt) and replayed: one launch instead of a few
+// hundred calls, and the graph, not the order of the streams, decides what runs side by side. The caller's stream
+// waits for the last download, so the call stays stream-ordered.
 extern "C" int bb_lsrk_run_host(bb_solver* s, double dt, int nsteps, const void* q_host_in,
                                 void* q_host_out, void* q_dev, void* res_dev, int use_graph,
                                 void* stream) {
@@ -798,28 +857,43 @@ extern "C" int bb_lsrk_run_host(bb_solver* s, double dt, int nsteps, const void*
   if (rc) return rc;
   rc = build_host_plan(s);
   if (rc) return rc;
-  HostPlan& P = *s->plan;
-  char* hout = static_cast<char*>(q_host_out);
-  // every stream starts after the caller's earlier work
-  BB_CUDA(s->ctx, cudaEventRecord(P.start_ev(), st));
-  BB_CUDA(s->ctx, cudaStreamWaitEvent(s->copy_stream, P.start_ev(), 0));
-  BB_CUDA(s->ctx, cudaStreamWaitEvent(s->down_stream, P.start_ev(), 0));
-  for (cudaStream_t x : s->stage_stream) BB_CUDA(s->ctx, cudaStreamWaitEvent(x, P.start_ev(), 0));
-  rc = host_plan_step(s, dt, q_dev, res_dev, 0, true, nsteps == 1,
-                      static_cast<const char*>(q_host_in), hout);
-  if (rc) return rc;
-  if (nsteps > 1) {
-    // the middle steps on the caller's stream once the first step is done everywhere
-    BB_CUDA(s->ctx, cudaEventRecord(P.mid_ev(), s->stage_stream[4]));
-    BB_CUDA(s->ctx, cudaStreamWaitEvent(st, P.mid_ev(), 0));
-    rc = run_steps(s, dt, nsteps - 2, q_dev, res_dev, use_graph, st, 1);
-    if (rc) return rc;
-    BB_CUDA(s->ctx, cudaEventRecord(P.mid_ev(), st));
-    for (cudaStream_t x : s->stage_stream) BB_CUDA(s->ctx, cudaStreamWaitEvent(x, P.mid_ev(), 0));
-    rc = host_plan_step(s, dt, q_dev, res_dev, (nsteps - 1) & 1, false, true, nullptr, hout);
-    if (rc) return rc;
+  if (!use_graph || nsteps != 1 || !pinned_host(q_host_in) || !pinned_host(q_host_out))
+    return enqueue_host_run(s, dt, nsteps, q_host_in, q_host_out, q_dev, res_dev, use_graph, st);
+  if (s->host_graph &&
+      (s->hg_in != q_host_in || s->hg_out != q_host_out || s->hg_q != q_dev ||
+       s->hg_res != res_dev || s->hg_dt != dt || s->hg_epb != s->epb ||
+       s->hg_epoch != s->ctx->config_epoch)) {
+    cudaGraphExecDestroy(s->host_graph);
+    s->host_graph = nullptr;
   }
-  BB_CUDA(s->ctx, cudaEventRecord(P.done_ev(), s->down_stream));
-  BB_CUDA(s->ctx, cudaStreamWaitEvent(st, P.done_ev(), 0));
+  if (!s->host_graph) {
+    cudaGraph_t g = nullptr;
+    BB_CUDA(s->ctx, cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
+    const int64_t launches = s->ctx->launches;
+    rc = enqueue_host_run(s, dt, 1, q_host_in, q_host_out, q_dev, res_dev, 0, s->cap_stream);
+    cudaError_t e = cudaStreamEndCapture(s->cap_stream, &g);
+    s->ctx->launches = launches;  // counted when the graph runs
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess)
+      return bb_fail(s->ctx, BB_ERR_CUDA, "host-path capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&s->host_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      s->host_graph = nullptr;
+      return bb_fail(s->ctx, BB_ERR_CUDA, "host-path instantiate: %s", cudaGetErrorString(e));
+    }
+    s->hg_in = q_host_in;
+    s->hg_out = q_host_out;
+    s->hg_q = q_dev;
+    s->hg_res = res_dev;
+    s->hg_dt = dt;
+    s->hg_epb = s->epb;
+    s->hg_epoch = s->ctx->config_epoch;
+  }
+  BB_CUDA(s->ctx, cudaGraphLaunch(s->host_graph, st));
+  s->ctx->launches += 6 * s->plan->C;  // C trace extractions and 5 C stage launches
   return BB_OK;
 }

@@ -152,7 +152,9 @@ int bb_solver_check(bb_solver* s, void* stream);
  * as it lands, each stage runs on a chunk once the previous stage has finished on the chunks
  * holding its neighbours (read once from conn), and a chunk goes down as soon as its last
  * stage is done, so both copy directions overlap the compute; with several steps the middle
- * ones run as whole launches on `stream`. The results are those of bb_lsrk_run. The call is
+ * ones run as whole launches on `stream`. One step with use_graph set and page-locked host
+ * buffers is captured into a graph on first use and replayed while the buffers, dt and tile
+ * stay the same. The results are those of bb_lsrk_run. The call is
  * stream-ordered: `stream` waits for the last download. The host buffers must stay valid
  * until then; pinned host memory is needed for the copies to overlap. q_host_in and
  * q_host_out may be the same buffer. */

@@ -154,10 +154,15 @@ def test_host_path_24_chunks_on_the_headline_tile(cuda, bb, nsteps):
     hin = q0.cpu().pin_memory()
     hout = torch.full_like(hin, float("nan")).pin_memory()
     qd, rd = torch.empty_like(q0), torch.zeros_like(q0)
-    for _ in range(2):  # the second call reuses the schedule and its events
+    for _ in range(2):  # the second call reuses the schedule (one step: its graph)
         s.run_host(hin, hout, qd, rd, step, nsteps)
         torch.cuda.synchronize()
         assert torch.equal(hout, qa.cpu()) and torch.equal(qd, qa) and torch.equal(rd, ra)
+    # pageable host buffers take the direct path; a new pinned output buffer a new graph
+    for out in (torch.full_like(hin, float("nan")), torch.full_like(hin, float("nan")).pin_memory()):
+        s.run_host(hin.clone(), out, qd, rd, step, nsteps)
+        torch.cuda.synchronize()
+        assert torch.equal(out, qa.cpu())
     s.check()
 
 
