@@ -61,6 +61,7 @@ SIGNATURES = {
     "bb_lsrk_run": (_I, [_P, _D, _I, _P, _P, _I, _P]),
     "bb_solver_check": (_I, [_P, _P]),
     "bb_lsrk_run_host": (_I, [_P, _D, _I, _P, _P, _P, _P, _I, _P]),
+    "bb_host_schedule": (_I, [_I64, _I, _P, _P, _P, _P, _P, _P, _P]),
     "bb_norms": (_I, [_P, _I, _I64, _I, _I, _P, _P, ctypes.POINTER(_D), _P]),
     "bb_mass_norms": (_I, [_P, _I, _I64, _I, _I, _P, _P, _P, ctypes.POINTER(_D), _P]),
     "bb_norms_noalloc": (_I, [_I, _I64, _I, _I, _P, _P, _P, _P]),

@@ -562,36 +562,24 @@ int ensure_host_streams(bb_solver* s) {
   return BB_OK;
 }
 
-// Builds bb_lsrk_run_host's schedule for the solver's tile size (see HostPlan). The chunk
-// neighbour graph comes from one download of the connectivity; entries that name no element
-// (the kernels report those) add no edge.
-int build_host_plan(bb_solver* s) {
-  if (s->plan && s->plan->epb == s->epb) return BB_OK;
-  if (s->plan) {
-    for (auto& e : s->plan->ev)
-      if (e) cudaEventDestroy(e);
-    delete s->plan;
-    s->plan = nullptr;
-  }
-  HostPlan* P = new (std::nothrow) HostPlan();
-  if (!P) return BB_ERR_NOMEM;
-  const int64_t K = s->K;
-  const int64_t ntiles = (K + s->epb - 1) / s->epb;
-  // up to 24 chunks of at least 8 tiles
-  const int C = (int)std::min<int64_t>(24, std::max<int64_t>(1, ntiles / 8));
-  P->epb = s->epb;
+// bb_lsrk_run_host's schedule (HostPlan without its events) for K elements in tiles of epb,
+// from a host copy of the packed connectivity: up to kHostMaxChunks chunks of at least 8
+// tiles, the chunk neighbour graph (chunk c touches chunk d when an element of c has a face
+// neighbour in d; entries that name no element, which the kernels report, add no edge), the
+// upload order (breadth-first from chunk 0, lower chunks first) and the launch order and
+// waits of each stage.
+constexpr int kHostMaxChunks = BB_HOST_MAX_CHUNKS;
+static_assert(kHostMaxChunks <= 64, "chunk neighbour sets are 64-bit masks");
+void plan_schedule(int64_t K, int epb, const int32_t* conn, HostPlan* P) {
+  const int64_t ntiles = (K + epb - 1) / epb;
+  const int C = (int)std::min<int64_t>(kHostMaxChunks, std::max<int64_t>(1, ntiles / 8));
+  P->epb = epb;
   P->C = C;
-  P->tb.resize(C + 1);
-  P->eb.resize(C + 1);
+  P->tb.assign(C + 1, 0);
+  P->eb.assign(C + 1, 0);
   for (int c = 0; c <= C; ++c) {
     P->tb[c] = ntiles * c / C;
-    P->eb[c] = std::min<int64_t>(K, P->tb[c] * s->epb);
-  }
-  std::vector<int32_t> conn((size_t)K * 4);
-  if (cudaMemcpy(conn.data(), s->conn, conn.size() * sizeof(int32_t), cudaMemcpyDefault) !=
-      cudaSuccess) {
-    delete P;
-    return bb_fail(s->ctx, BB_ERR_CUDA, "connectivity download failed");
+    P->eb[c] = std::min<int64_t>(K, P->tb[c] * epb);
   }
   std::vector<uint64_t> nb(C, 0);  // neighbour chunks of each chunk (itself included)
   for (int c = 0; c < C; ++c) {
@@ -605,8 +593,8 @@ int build_host_plan(bb_solver* s) {
         nb[cn] |= uint64_t(1) << c;
       }
   }
-  // upload order: breadth-first from chunk 0, lower chunks first
   std::vector<int> pos(C, -1);
+  P->up.clear();
   for (int root = 0; root < C; ++root) {
     if (pos[root] >= 0) continue;
     size_t head = P->up.size();
@@ -621,7 +609,8 @@ int build_host_plan(bb_solver* s) {
         }
     }
   }
-  // stage 0 (of a step fed by the uploads): a chunk may run once every neighbour chunk is in
+  // stage 0 (of a step fed by the uploads): a chunk may run once every neighbour chunk is in;
+  // stage s: once stage s-1 has run on every neighbour chunk (its stream runs in order)
   std::vector<int> key(C), idx(C);
   auto sort_by = [&](std::vector<int>& order, const std::vector<int>& tie) {
     order.resize(C);
@@ -638,6 +627,7 @@ int build_host_plan(bb_solver* s) {
   sort_by(P->order[0], pos);
   P->ready0.resize(C);
   for (int i = 0; i < C; ++i) P->ready0[i] = key[P->order[0][i]];
+  P->wait[0].assign(C, -1);
   for (int st = 1; st < 5; ++st) {
     for (int i = 0; i < C; ++i) idx[P->order[st - 1][i]] = i;
     for (int c = 0; c < C; ++c) {
@@ -649,6 +639,28 @@ int build_host_plan(bb_solver* s) {
     P->wait[st].resize(C);
     for (int i = 0; i < C; ++i) P->wait[st][i] = key[P->order[st][i]];
   }
+}
+
+// Builds (or keeps) bb_lsrk_run_host's schedule for the solver's tile size, with its events;
+// the connectivity is read once from the device.
+int build_host_plan(bb_solver* s) {
+  if (s->plan && s->plan->epb == s->epb) return BB_OK;
+  if (s->plan) {
+    for (auto& e : s->plan->ev)
+      if (e) cudaEventDestroy(e);
+    delete s->plan;
+    s->plan = nullptr;
+  }
+  HostPlan* P = new (std::nothrow) HostPlan();
+  if (!P) return BB_ERR_NOMEM;
+  std::vector<int32_t> conn((size_t)s->K * 4);
+  if (cudaMemcpy(conn.data(), s->conn, conn.size() * sizeof(int32_t), cudaMemcpyDefault) !=
+      cudaSuccess) {
+    delete P;
+    return bb_fail(s->ctx, BB_ERR_CUDA, "connectivity download failed");
+  }
+  plan_schedule(s->K, s->epb, conn.data(), P);
+  const int C = P->C;
   P->ev.assign((size_t)6 * C + 3, nullptr);
   for (auto& e : P->ev)
     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
@@ -895,5 +907,32 @@ extern "C" int bb_lsrk_run_host(bb_solver* s, double dt, int nsteps, const void*
   }
   BB_CUDA(s->ctx, cudaGraphLaunch(s->host_graph, st));
   s->ctx->launches += 6 * s->plan->C;  // C trace extractions and 5 C stage launches
+  return BB_OK;
+}
+
+// The schedule bb_lsrk_run_host uses for K elements in tiles of epb with this (host) packed
+// connectivity; host-only. Arrays hold at least BB_HOST_MAX_CHUNKS (+1 for chunk_tiles)
+// entries per row: chunk_tiles[c] = first tile of chunk c (chunk_tiles[C] = tile count),
+// up = upload order, order[s*max + i] = i-th chunk stage s launches, ready0[i] = last upload
+// position order[0][i] needs, wait[s*max + i] = launch of stage s-1 that order[s][i] waits for.
+extern "C" int bb_host_schedule(int64_t K, int epb, const int32_t* conn_host, int* nchunks,
+                                int64_t* chunk_tiles, int* up, int* order, int* ready0,
+                                int* wait) {
+  if (K < 1 || epb < 1 || !conn_host || !nchunks || !chunk_tiles || !up || !order || !ready0 ||
+      !wait)
+    return BB_ERR_ARG;
+  HostPlan P;
+  plan_schedule(K, epb, conn_host, &P);
+  const int C = P.C, M = BB_HOST_MAX_CHUNKS;
+  *nchunks = C;
+  for (int c = 0; c <= C; ++c) chunk_tiles[c] = P.tb[c];
+  for (int i = 0; i < C; ++i) {
+    up[i] = P.up[i];
+    ready0[i] = P.ready0[i];
+    for (int st = 0; st < 5; ++st) {
+      order[st * M + i] = P.order[st][i];
+      wait[st * M + i] = P.wait[st][i];
+    }
+  }
   return BB_OK;
 }

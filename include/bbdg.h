@@ -162,6 +162,18 @@ int bb_lsrk_run_host(bb_solver* s, double dt, int nsteps, const void* q_host_in,
                      void* q_host_out, void* q_dev, void* res_dev, int use_graph,
                      void* stream);
 
+/* The chunk schedule of bb_lsrk_run_host for K elements in tiles of epb elements, from a
+ * host copy of the packed connectivity (as bb_solver_create); host-only, no CUDA call.
+ * *nchunks = C <= BB_HOST_MAX_CHUNKS. chunk_tiles[0..C]: chunk c is tiles
+ * [chunk_tiles[c], chunk_tiles[c+1]). up[p]: the chunk uploaded p-th. order[s*BB_HOST_MAX_CHUNKS
+ * + i]: the chunk LSRK stage s launches i-th. ready0[i]: the last upload position
+ * order[0][i] needs (its traces extracted). wait[s*BB_HOST_MAX_CHUNKS + i] (s >= 1): the
+ * launch index of stage s-1 that order[s][i] waits for (launches of one stage run in order;
+ * -1 for s = 0). For a test or a tool that checks the schedule's dependencies. */
+#define BB_HOST_MAX_CHUNKS 24
+int bb_host_schedule(int64_t K, int epb, const int32_t* conn_host, int* nchunks,
+                     int64_t* chunk_tiles, int* up, int* order, int* ready0, int* wait);
+
 /* ---- StartUpDG MeshData import (host functions, no device work) -------------------------
  * conn_out[e*4+f] (the packed connectivity of bb_solver_create) from StartUpDG's
  * rd.Fmask (4*Nfp volume indices, faces in reference order) and md.mapP (K*4*Nfp global
