@@ -3,8 +3,10 @@
 // degree-specialised FP32 kernels in bbdg_stage_fast.cu; this file owns trace buffers,
 // kernel selection, LSRK stepping and CUDA graphs.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
+#include <new>
 #include <vector>
 
 #include "bbdg_internal.cuh"
@@ -653,13 +655,24 @@ int build_host_plan(bb_solver* s) {
   }
   HostPlan* P = new (std::nothrow) HostPlan();
   if (!P) return BB_ERR_NOMEM;
-  std::vector<int32_t> conn((size_t)s->K * 4);
+  std::vector<int32_t> conn;
+  try {
+    conn.resize((size_t)s->K * 4);
+  } catch (const std::bad_alloc&) {
+    delete P;
+    return bb_fail(s->ctx, BB_ERR_NOMEM, "host schedule allocation failed");
+  }
   if (cudaMemcpy(conn.data(), s->conn, conn.size() * sizeof(int32_t), cudaMemcpyDefault) !=
       cudaSuccess) {
     delete P;
     return bb_fail(s->ctx, BB_ERR_CUDA, "connectivity download failed");
   }
-  plan_schedule(s->K, s->epb, conn.data(), P);
+  try {
+    plan_schedule(s->K, s->epb, conn.data(), P);
+  } catch (const std::bad_alloc&) {
+    delete P;
+    return bb_fail(s->ctx, BB_ERR_NOMEM, "host schedule allocation failed");
+  }
   const int C = P->C;
   P->ev.assign((size_t)6 * C + 3, nullptr);
   for (auto& e : P->ev)
@@ -701,27 +714,29 @@ int host_plan_step(bb_solver* s, double dt, void* q, void* res, int par, bool up
   struct Item {
     int level, stream, seq, kind, stage, i;
   };
-  std::vector<Item> items;
-  items.reserve((size_t)8 * C);
+  // at most 8 C items (C <= kHostMaxChunks); levels of the uploads and stage launches
+  std::array<Item, 8 * kHostMaxChunks> items;
+  size_t nitems = 0;
   // streams: 0 uploads, 1..5 stages 0..4, 6 downloads
-  std::vector<int> lv_up(C), lv_stage((size_t)5 * C);
+  std::array<int, kHostMaxChunks> lv_up{};
+  std::array<int, 5 * kHostMaxChunks> lv_stage{};
   int seq = 0, last = -1;
   if (upload)
     for (int p = 0; p < C; ++p) {
       lv_up[p] = p;
-      items.push_back({p, 0, seq++, UP, 0, p});
+      items[nitems++] = Item{p, 0, seq++, UP, 0, p};
     }
   int i = 0;
   last = -1;
   for (int p = 0; p < C; ++p) {
     if (upload) {
       last = std::max(last + 1, lv_up[p] + 1);
-      items.push_back({last, 1, seq++, EXTRACT, 0, p});
+      items[nitems++] = Item{last, 1, seq++, EXTRACT, 0, p};
     }
     for (; i < C && (!upload || P.ready0[i] <= p); ++i) {
       last = last + 1;
       lv_stage[i] = last;
-      items.push_back({last, 1, seq++, STAGE, 0, i});
+      items[nitems++] = Item{last, 1, seq++, STAGE, 0, i};
     }
   }
   for (int st = 1; st < 5; ++st) {
@@ -729,23 +744,24 @@ int host_plan_step(bb_solver* s, double dt, void* q, void* res, int par, bool up
     for (int j = 0; j < C; ++j) {
       last = std::max(last + 1, lv_stage[(size_t)(st - 1) * C + P.wait[st][j]] + 1);
       lv_stage[(size_t)st * C + j] = last;
-      items.push_back({last, 1 + st, seq++, STAGE, st, j});
+      items[nitems++] = Item{last, 1 + st, seq++, STAGE, st, j};
     }
   }
   if (download) {
     last = -1;
     for (int j = 0; j < C; ++j) {
       last = std::max(last + 1, lv_stage[(size_t)4 * C + j] + 1);
-      items.push_back({last, 6, seq++, DOWN, 4, j});
+      items[nitems++] = Item{last, 6, seq++, DOWN, 4, j};
     }
   }
-  std::sort(items.begin(), items.end(), [](const Item& a, const Item& b) {
+  std::sort(items.begin(), items.begin() + nitems, [](const Item& a, const Item& b) {
     return a.level != b.level ? a.level < b.level
                               : a.stream != b.stream ? a.stream < b.stream : a.seq < b.seq;
   });
   cudaStream_t* ss = s->stage_stream;
   int waited[5] = {-1, -1, -1, -1, -1};
-  for (const Item& it : items) {
+  for (size_t k = 0; k < nitems; ++k) {
+    const Item& it = items[k];
     int rc = BB_OK;
     if (it.kind == UP) {
       const int c = P.up[it.i];
@@ -922,7 +938,11 @@ extern "C" int bb_host_schedule(int64_t K, int epb, const int32_t* conn_host, in
       !wait)
     return BB_ERR_ARG;
   HostPlan P;
-  plan_schedule(K, epb, conn_host, &P);
+  try {
+    plan_schedule(K, epb, conn_host, &P);
+  } catch (const std::bad_alloc&) {
+    return BB_ERR_NOMEM;
+  }
   const int C = P.C, M = BB_HOST_MAX_CHUNKS;
   *nchunks = C;
   for (int c = 0; c <= C; ++c) chunk_tiles[c] = P.tb[c];
