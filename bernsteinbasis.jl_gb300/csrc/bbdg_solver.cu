@@ -28,23 +28,29 @@ __global__ void __launch_bounds__(kThreads) stage_kernel(StageParams<T> P, TileL
 }
 
 // Writes every face trace (all faces) of elements [e_begin, e_end) of q into the trace buffer.
+// An element's 4 NF Nfp trace entries are contiguous in the buffer; each block first decodes
+// entry i into (field, volume node) once (shared table), then copies element after element:
+// one table read, one gather from the element's field rows, one coalesced store per entry.
 template <class T, int NF>
 __global__ void extract_traces_kernel(DegTables tab, const uint32_t* __restrict__ gtab,
                                       int64_t K, const T* __restrict__ q, T* __restrict__ tr,
                                       int64_t e_begin, int64_t e_end) {
-  const int Np = tab.Np, Nfp = tab.Nfp;
+  extern __shared__ uint32_t s_src[];  // entry i: field << 16 | volume node
+  const int Np = tab.Np, Nfp = tab.Nfp, W = 4 * NF * Nfp;
   const uint16_t* fvol = reinterpret_cast<const uint16_t*>(gtab + tab.o_fvol);
-  const int64_t first = e_begin * 4 * NF * Nfp;
-  const int64_t total = (e_end - e_begin) * 4 * NF * Nfp;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t it = first + i;
-    const int64_t e = it / (4 * NF * Nfp);
-    int rem = (int)(it - e * 4 * NF * Nfp);
-    const int f = rem / (NF * Nfp);
-    rem -= f * NF * Nfp;
-    const int fld = rem / Nfp, a = rem - fld * Nfp;
-    tr[it] = q[((size_t)fld * K + e) * Np + fvol[f * Nfp + a]];
+  for (int i = threadIdx.x; i < W; i += blockDim.x) {
+    const int f = i / (NF * Nfp), rem = i - f * NF * Nfp, fld = rem / Nfp, a = rem - fld * Nfp;
+    s_src[i] = ((uint32_t)fld << 16) | fvol[f * Nfp + a];
+  }
+  __syncthreads();
+  const size_t field = (size_t)K * Np;
+  for (int64_t e = e_begin + blockIdx.x; e < e_end; e += gridDim.x) {
+    const T* qe = q + (size_t)e * Np;
+    T* te = tr + (size_t)e * W;
+    for (int i = threadIdx.x; i < W; i += blockDim.x) {
+      const uint32_t v = s_src[i];
+      te[i] = qe[(v >> 16) * field + (v & 0xffffu)];
+    }
   }
 }
 
@@ -251,30 +257,26 @@ int launch_stage(bb_solver* s, int mode, int stage, double dt, void* q, void* re
 int launch_extract(bb_solver* s, const void* q, void* tr, cudaStream_t st, int64_t e0 = 0,
                    int64_t e1 = -1) {
   if (e1 < 0) e1 = s->K;
-  const int64_t total = (e1 - e0) * 4 * s->nf * s->tab->Nfp;
-  int64_t grid = (total + 255) / 256;
-  if (grid > (int64_t)s->ctx->num_sms * 16) grid = (int64_t)s->ctx->num_sms * 16;
-  if (grid < 1) grid = 1;
+  if (e1 <= e0) return BB_OK;
+  int64_t grid = e1 - e0;
+  if (grid > (int64_t)s->ctx->num_sms * 8) grid = (int64_t)s->ctx->num_sms * 8;
   const DegTables& t = *s->tab;
+  const size_t smem = (size_t)4 * s->nf * t.Nfp * sizeof(uint32_t);
+#define BB_EXTRACT(T_, NF_)                                                                \
+  extract_traces_kernel<T_, NF_><<<(int)grid, 256, smem, st>>>(t, t.d_words, s->K,         \
+                                                                (const T_*)q, (T_*)tr, e0, e1)
   if (s->dtype == BB_F64) {
-    if (s->nf == 4)
-      extract_traces_kernel<double, 4><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr, e0, e1);
-    else if (s->nf == 1)
-      extract_traces_kernel<double, 1><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr, e0, e1);
-    else if (s->nf == 3)
-      extract_traces_kernel<double, 3><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr, e0, e1);
-    else
-      extract_traces_kernel<double, 6><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const double*)q, (double*)tr, e0, e1);
+    if (s->nf == 4) BB_EXTRACT(double, 4);
+    else if (s->nf == 1) BB_EXTRACT(double, 1);
+    else if (s->nf == 3) BB_EXTRACT(double, 3);
+    else BB_EXTRACT(double, 6);
   } else {
-    if (s->nf == 4)
-      extract_traces_kernel<float, 4><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr, e0, e1);
-    else if (s->nf == 1)
-      extract_traces_kernel<float, 1><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr, e0, e1);
-    else if (s->nf == 3)
-      extract_traces_kernel<float, 3><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr, e0, e1);
-    else
-      extract_traces_kernel<float, 6><<<(int)grid, 256, 0, st>>>(t, t.d_words, s->K, (const float*)q, (float*)tr, e0, e1);
+    if (s->nf == 4) BB_EXTRACT(float, 4);
+    else if (s->nf == 1) BB_EXTRACT(float, 1);
+    else if (s->nf == 3) BB_EXTRACT(float, 3);
+    else BB_EXTRACT(float, 6);
   }
+#undef BB_EXTRACT
   return bb_check_launch(s->ctx, "extract_traces_kernel");
 }
 
