@@ -136,7 +136,11 @@ class DGSolver:
     def run_host(self, q_host_in: torch.Tensor, q_host_out: torch.Tensor, q_dev: torch.Tensor,
                  res_dev: torch.Tensor, dt: float, nsteps: int, graph: bool = True,
                  stream=None) -> None:
-        """Host-in/host-out variant: copy q in, advance, copy q out (stream-ordered)."""
+        """Host-in/host-out variant: copy q in, advance, copy q out (stream-ordered).
+
+        bb_lsrk_run_host pipelines the copies with the stages over element chunks; pass
+        page-locked tensors (``Tensor.pin_memory()``) for the copies to overlap and, with
+        ``graph`` and one step, for the call to be captured once and replayed."""
         self._check_state(q_dev, res_dev)
         for t in (q_host_in, q_host_out):
             if t.is_cuda or t.shape != q_dev.shape or t.dtype != self.dtype or not t.is_contiguous():
