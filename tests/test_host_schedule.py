@@ -128,3 +128,22 @@ def test_the_checker_rejects_a_lowered_wait(bb):
     planted = dict(sch, wait=sch["wait"].copy())
     planted["wait"][2][i] -= 1
     assert any("stage 2" in v for v in violations(planted, conn, 4))
+
+
+def test_schedule_edge_cases(bb):
+    """Fewer than 16 tiles: one chunk, and every order and wait degenerate; a tile that does
+    not divide K (the generic kernel's ragged last tile): chunks still cover every tile;
+    connectivity entries that name no element (which the kernels report) add no edge."""
+    conn = bb.uniform_tet_mesh(2).conn.reshape(-1, 4)          # K = 48
+    one = schedule(bb, conn, 4)                                # 12 tiles
+    assert one["C"] == 1 and one["tiles"].tolist() == [0, 12]
+    assert violations(one, conn, 4) == []
+    conn3 = bb.uniform_tet_mesh(3).conn.reshape(-1, 4)         # K = 162
+    ragged = schedule(bb, conn3, 5)                            # 33 tiles, the last of 2
+    assert ragged["C"] == 4 and ragged["tiles"][-1] == 33
+    assert violations(ragged, conn3, 5) == []
+    bad = conn3.copy()
+    bad[::7, 1] = (bad[::7, 1] & 31) | (1 << 26)               # neighbour index past K
+    bad[::11, 2] = -1
+    sch = schedule(bb, bad, 2)
+    assert violations(sch, bad, 2) == []
